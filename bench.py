@@ -1,0 +1,307 @@
+"""Benchmark: particle-substeps/s of the column-collapse workload on GB300.
+
+A "step" is one substep of the reference's GranularSystem::step (grid
+build, 3 stabilisation + 4 Jacobi sweeps, finalize, upsampling of 4 render
+points per particle, surface detection and merge/split on the integer
+ledger) over 8,388,608 particles resident in HBM.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl mine|reference]
+
+N > 1 runs N independent replicas (one per rank, launched by torchrun); the
+path has no exchange step.  `--impl reference` times the CPU restatement of
+the reference's path (the reference itself is CUDA-only, it has no CPU
+implementation) on a bounded sample of the same workload.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-substeps/s"
+WORKLOAD = "column collapse 128x256x256 (8,388,608 particles, r=0.002, 2x1x1 box, dt=1/120 x 4 substeps, " \
+           "3+4 sweeps, merge/split to mass 8, 4 render points/particle)"
+SAMPLE_COUNTS = (64, 64, 64)
+SAMPLE_NOTE = "64x64x64 sub-lattice (262,144 particles) of the same column scene (same box, grid, walls, " \
+              "parameters), one oracle substep per step"
+# algorithmic bytes per particle of one Jacobi iteration: read x* and radius
+# (16 B), write x* (12 B)
+SWEEP_BYTES_PER_PARTICLE = 28
+
+
+def _dist():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.out = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.out, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        time.sleep(0.3)
+
+    def stop(self):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        self.out.flush()
+        rows = []
+        with open(self.out.name) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.out.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def measured_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def ncu_traffic():
+    """Per-launch DRAM bytes of the sweep kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "sweep_traffic.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return d
+    except (OSError, ValueError):
+        return None
+
+
+def cpu_sample(steps: int, warmup: int, fp64: bool = True):
+    """Times the oracle (CPU restatement) on the bounded sample."""
+    from granular_gpu_gb300 import workloads
+    from oracle import oracle as orc
+    desc = workloads.column_collapse(counts=SAMPLE_COUNTS)
+    o = orc.OracleSystem(desc, fp64=fp64)
+    o.step(warmup)
+    units = 0
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        units += o.size()
+        o.step(1)
+    dt = time.perf_counter() - t0
+    threads = orc.threads()
+    o.close()
+    return units / dt, threads, dt
+
+
+def run_reference(args):
+    rank, world, _ = _dist()
+    if rank != 0:
+        return 0
+    value, threads, dt = cpu_sample(args.steps, args.warmup)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * dt / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": {"workload": WORKLOAD, "sample": SAMPLE_NOTE},
+        "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "port",
+                         "sample": SAMPLE_NOTE},
+        "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_mine(args):
+    import torch
+    import granular_gpu_gb300 as gg
+    from granular_gpu_gb300 import workloads
+
+    rank, world, local = _dist()
+    dist_on = world > 1
+    if dist_on:
+        import torch.distributed as tdist
+        tdist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    desc = workloads.column_collapse(seed=42 + rank)
+    n0 = desc["n_particles"]
+    sysg = gg.GranularSystem(**workloads.system_kwargs(desc), device=local)
+    stream = torch.cuda.ExternalStream(sysg.stream, device=local)
+    for _ in range(args.warmup):
+        sysg.step(1)
+    sysg.synchronize()
+
+    def barrier():
+        if dist_on:
+            tdist.barrier()
+
+    # ---- device-resident timed region
+    sampler = ClockSampler(local)
+    sampler.start()
+    barrier()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    sysg.profile_begin()
+    launches0 = sysg.stats()["launches"] if "launches" in sysg.stats() else 0
+    units = 0
+    ev0.record(stream)
+    for _ in range(args.steps):
+        units += sysg.size()
+        sysg.step(1)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    prof = sysg.profile_end()
+    clocks = sampler.stop()
+    ms = ev0.elapsed_time(ev1)
+    launches = sysg.stats().get("launches", 0) - launches0
+    t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+    u = torch.tensor([units], dtype=torch.float64, device="cuda")
+    if dist_on:
+        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+        tdist.all_reduce(u, op=tdist.ReduceOp.SUM)
+    ms_max = float(t.item())
+    total_units = float(u.item())
+    value = total_units / (ms_max / 1000.0)
+
+    # ---- end to end through the C ABI with pinned host buffers
+    n = sysg.size()
+    nu = sysg.upsampled_size()
+    hp = torch.empty((n, 3), dtype=torch.float32, pin_memory=True).numpy()
+    hv = torch.empty((n, 3), dtype=torch.float32, pin_memory=True).numpy()
+    hu = torch.empty((nu, 3), dtype=torch.float32, pin_memory=True).numpy()
+    sysg.read(gg.FIELD_POS, out=hp)
+    sysg.read(gg.FIELD_VEL, out=hv)
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e2e_units = 0
+    h2d = d2h = 0
+    for _ in range(args.steps):
+        m = sysg.size()
+        if hp.shape[0] != m:
+            hp = torch.empty((m, 3), dtype=torch.float32, pin_memory=True).numpy()
+            hv = torch.empty((m, 3), dtype=torch.float32, pin_memory=True).numpy()
+            sysg.read(gg.FIELD_POS, out=hp)
+            sysg.read(gg.FIELD_VEL, out=hv)
+        sysg.write(gg.FIELD_POS, hp)
+        sysg.write(gg.FIELD_VEL, hv)
+        h2d += 2 * hp.nbytes
+        e2e_units += m
+        sysg.step(1)
+        m = sysg.size()
+        if hp.shape[0] != m:
+            hp = torch.empty((m, 3), dtype=torch.float32, pin_memory=True).numpy()
+            hv = torch.empty((m, 3), dtype=torch.float32, pin_memory=True).numpy()
+        sysg.read(gg.FIELD_POS, out=hp)
+        sysg.read(gg.FIELD_VEL, out=hv)
+        sysg.read(gg.FIELD_POS, gg.SET_UPSAMPLED, out=hu)
+        d2h += 2 * hp.nbytes + hu.nbytes
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    te = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
+    ue = torch.tensor([e2e_units], dtype=torch.float64, device="cuda")
+    if dist_on:
+        tdist.all_reduce(te, op=tdist.ReduceOp.MAX)
+        tdist.all_reduce(ue, op=tdist.ReduceOp.SUM)
+    e2e_value = float(ue.item()) / float(te.item())
+
+    # ---- roofline of the dominant kernel class
+    dom = max(prof.items(), key=lambda kv: kv[1]["ms"])
+    sweep = prof["sweep"]
+    peak, peak_kind = measured_peak()
+    avg_ms = sweep["ms"] / max(sweep["launches"], 1)
+    units_per_launch = sweep["units"] / max(sweep["launches"], 1)
+    algo_bytes = SWEEP_BYTES_PER_PARTICLE * units_per_launch
+    achieved = algo_bytes / (avg_ms / 1000.0) / 1e9
+    tr = ncu_traffic()
+    traffic = None
+    if tr and tr.get("particles"):
+        traffic = float(tr["dram_bytes_per_launch"]) * units_per_launch / float(tr["particles"])
+    total_ms = sum(v["ms"] for v in prof.values())
+    shares = {k: round(v["ms"] / total_ms, 4) for k, v in prof.items() if v["launches"]}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "particles": n0, "upsampled": desc["n_upsampled"],
+                   "boundary": desc["n_boundary"], "cells": int(np.prod(desc["cell_size"])),
+                   "l2": "inputs larger than L2 (about 1.9 GB of particle state per step)",
+                   "parallelism": f"replicas x{world}"},
+        "roofline": {"bound": "hbm", "kernel": "sweep", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                     "algorithmic_bytes_per_particle": SWEEP_BYTES_PER_PARTICLE,
+                     "avg_launch_ms": avg_ms, "dominant_class": dom[0], "shares": shares},
+        "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d // max(args.steps, 1),
+                "d2h_bytes_per_step": d2h // max(args.steps, 1)},
+        "gpu_launches": int(launches),
+        "clocks": clocks,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cv, threads, _ = cpu_sample(steps=args.cpu_steps, warmup=1)
+        line["cpu_baseline"] = {"value": cv, "unit": METRIC, "cores": threads, "kind": "port",
+                                "sample": SAMPLE_NOTE + f", {args.cpu_steps} timed substeps, FP64 build"}
+    sysg.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist_on:
+        tdist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["mine", "reference"], default="mine")
+    ap.add_argument("--cpu-steps", type=int, default=4)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    import __graft_entry__
+    __graft_entry__.build()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_mine(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,349 @@
+"""granular_gpu_gb300 — GB300-native granular substep path behind a C ABI.
+
+Python mirror of the reference's GranularSystem surface
+(src/GranularSystem.hpp:8-56, src/Particles.hpp, src/GranularParticles.hpp),
+built only on libgg.so (include/gg.h).  There is no CPU fallback: every
+call runs the CUDA library and raises if it is missing.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi
+from .abi import (FIELD_ADAPTIVE_LAST_STEP, FIELD_CELL_KEY, FIELD_CELL_START,  # noqa: F401
+                  FIELD_CONTACTS, FIELD_IS_ANIMATED, FIELD_MASS, FIELD_MASS_UNITS, FIELD_MERGE,
+                  FIELD_MERGE_COUNT, FIELD_MERGE_VELOCITY, FIELD_NUM_CONSTRAINTS, FIELD_PERM,
+                  FIELD_POS, FIELD_REMOVE, FIELD_SURFACE, FIELD_SURFACE_DISTANCE, FIELD_VEL,
+                  SET_BOUNDARY, SET_GRANULAR, SET_UPSAMPLED, default_params)
+
+__all__ = ["GranularSystem", "GranularError", "Grid", "scene_build", "default_params", "lib"]
+
+_LIB = None
+
+
+def lib() -> C.CDLL:
+    """The loaded libgg.so (raises abi.NativeLibraryMissing when unbuilt)."""
+    global _LIB
+    if _LIB is None:
+        _LIB = abi.load_library()
+    return _LIB
+
+
+class GranularError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{abi.STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+
+
+def _check(rc: int):
+    if rc != abi.GG_OK:
+        msg = lib().gg_last_error()
+        raise GranularError(rc, msg.decode() if msg else "")
+
+
+def _f32(a, comp=3):
+    return np.ascontiguousarray(np.asarray(a, dtype=np.float32).reshape(-1, comp))
+
+
+def _fptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_float)) if a is not None else None
+
+
+def _iptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int32)) if a is not None else None
+
+
+class ParticleSet:
+    """get_*_ptr() readers of one particle set (Particles.hpp:18-20,
+    GranularParticles.hpp:19-26), copying to host arrays."""
+
+    def __init__(self, system: "GranularSystem", which: int):
+        self._s = system
+        self._set = which
+
+    def size(self) -> int:
+        return self._s._size(self._set)
+
+    def get_pos(self):
+        return self._s.read(FIELD_POS, self._set)
+
+    def get_vel(self):
+        return self._s.read(FIELD_VEL, self._set)
+
+    def get_mass(self):
+        return self._s.read(FIELD_MASS, self._set)
+
+    def get_surface(self):
+        return self._s.read(FIELD_SURFACE, self._set)
+
+    def get_surface_distance(self):
+        return self._s.read(FIELD_SURFACE_DISTANCE, self._set)
+
+    def get_adaptive_last_step(self):
+        return self._s.read(FIELD_ADAPTIVE_LAST_STEP, self._set)
+
+    def get_particle_2_cell(self):
+        return self._s.read(FIELD_CELL_KEY, self._set)
+
+    def get_is_animated(self):
+        return self._s.read(FIELD_IS_ANIMATED, self._set)
+
+
+class Solver:
+    """GranularSystem::get_solver() (GranularSystem.hpp:56)."""
+
+    def __init__(self, system: "GranularSystem"):
+        self._s = system
+
+    def save_particle_stats(self, filename: str):
+        _check(lib().gg_save_particle_stats(self._s._h, filename.encode()))
+
+    def trigger_explosion(self, explosion_force: float):
+        _check(lib().gg_trigger_explosion(self._s._h, float(explosion_force)))
+
+    def get_buffer_merge_count(self):
+        return self._s.read(FIELD_MERGE_COUNT)
+
+    def get_buffer_merge(self):
+        return self._s.read(FIELD_MERGE)
+
+    def get_buffer_remove(self):
+        return self._s.read(FIELD_REMOVE)
+
+
+class GranularSystem:
+    """GranularSystem(particles, boundary, upsampled, space_size, cell_length,
+    dt, g, cell_size, density, upsampled_radius, is_move_boundary,
+    is_adaptive) — GranularSystem.hpp:8-14.  Construction runs one step, as
+    the reference's constructor does (GranularSystem.cu:62)."""
+
+    def __init__(self, particles, boundary_particles, upsampled_particles, space_size, cell_length,
+                 dt, g, cell_size, density, upsampled_radius=0.005, is_move_boundary=False,
+                 is_adaptive=1, *, masses=None, boundary_animated=None, params=None, device=0,
+                 max_particles=0, skip_initial_step=False, stream=None):
+        self._h = None
+        l = lib()
+        p = _f32(particles)
+        b = _f32(boundary_particles) if boundary_particles is not None and len(boundary_particles) else None
+        u = _f32(upsampled_particles) if upsampled_particles is not None and len(upsampled_particles) else None
+        m = np.ascontiguousarray(masses, dtype=np.float32) if masses is not None else None
+        a = np.ascontiguousarray(boundary_animated, dtype=np.int32) if boundary_animated is not None else None
+        d = abi.gg_desc()
+        d.particles, d.n_particles = _fptr(p), p.shape[0]
+        d.masses = _fptr(m)
+        d.boundary, d.n_boundary = _fptr(b), 0 if b is None else b.shape[0]
+        d.boundary_animated = _iptr(a)
+        d.upsampled, d.n_upsampled = _fptr(u), 0 if u is None else u.shape[0]
+        for i in range(3):
+            d.space_size[i] = float(space_size[i])
+            d.gravity[i] = float(g[i])
+            d.cell_size[i] = int(cell_size[i])
+        d.cell_length, d.dt, d.density = float(cell_length), float(dt), float(density)
+        d.upsampled_radius = float(upsampled_radius)
+        d.is_move_boundary, d.is_adaptive = int(bool(is_move_boundary)), int(is_adaptive)
+        d.skip_initial_step, d.device = int(bool(skip_initial_step)), int(device)
+        d.max_particles = int(max_particles)
+        d.stream = stream
+        d.params = params if params is not None else default_params()
+        h = C.c_void_p()
+        _check(l.gg_create(C.byref(d), C.byref(h)))
+        self._h = h
+        self.cell_size = tuple(int(x) for x in cell_size)
+
+    @classmethod
+    def from_scene(cls, json_path: str, params=None, device=0, base_dir=None, max_particles=0,
+                   skip_initial_step=False, stream=None) -> "GranularSystem":
+        """loadSceneConfig + init_granular_system + constructor
+        (main.cu:123-167, 746-1173)."""
+        self = cls.__new__(cls)
+        self._h = None
+        ov = abi.gg_overrides()
+        if params is not None:
+            ov.has_params, ov.params = 1, params
+        ov.device, ov.max_particles, ov.stream = int(device), int(max_particles), stream
+        ov.skip_initial_step = int(bool(skip_initial_step))
+        ov.base_dir = base_dir.encode() if base_dir else None
+        h = C.c_void_p()
+        _check(lib().gg_create_from_scene(json_path.encode(), C.byref(ov), C.byref(h)))
+        self._h = h
+        cs = (C.c_int32 * 3)()
+        _check(lib().gg_grid_dims(h, cs, None))
+        self.cell_size = tuple(cs)
+        return self
+
+    # -- GranularSystem::step and sizes ---------------------------------
+    def step(self, n_substeps: int = 1) -> int:
+        _check(lib().gg_step(self._h, int(n_substeps)))
+        return 1
+
+    def synchronize(self):
+        _check(lib().gg_synchronize(self._h))
+
+    def _size(self, which):
+        n = C.c_int64()
+        _check(lib().gg_size(self._h, which, C.byref(n)))
+        return n.value
+
+    def size(self) -> int:
+        return self._size(SET_GRANULAR)
+
+    def upsampled_size(self) -> int:
+        return self._size(SET_UPSAMPLED)
+
+    def boundary_size(self) -> int:
+        return self._size(SET_BOUNDARY)
+
+    def total_size(self) -> int:
+        return self.size() + self.boundary_size() + self.upsampled_size()
+
+    def get_particles(self) -> ParticleSet:
+        return ParticleSet(self, SET_GRANULAR)
+
+    def get_boundaries(self) -> ParticleSet:
+        return ParticleSet(self, SET_BOUNDARY)
+
+    def get_upsampled(self) -> ParticleSet:
+        return ParticleSet(self, SET_UPSAMPLED)
+
+    def get_solver(self) -> Solver:
+        return Solver(self)
+
+    # -- field access -----------------------------------------------------
+    def read(self, field: int, which: int = SET_GRANULAR, out=None):
+        dt, comp = abi.FIELD_LAYOUT[field]
+        n = C.c_int64()
+        _check(lib().gg_read(self._h, which, field, None, 0, C.byref(n)))
+        cnt = n.value
+        if out is None:
+            out = np.empty((max(cnt, 1), comp), dtype=dt)
+        _check(lib().gg_read(self._h, which, field, out.ctypes.data_as(C.c_void_p), out.shape[0], C.byref(n)))
+        out = out[:cnt]
+        return out[:, 0] if comp == 1 else out
+
+    def write(self, field: int, data, which: int = SET_GRANULAR):
+        a = _f32(data)
+        _check(lib().gg_write(self._h, which, field, a.ctypes.data_as(C.c_void_p), a.shape[0]))
+
+    def device_ptr(self, field: int, which: int = SET_GRANULAR):
+        p, n, st = C.c_void_p(), C.c_int64(), C.c_int32()
+        _check(lib().gg_device_ptr(self._h, which, field, C.byref(p), C.byref(n), C.byref(st)))
+        return p.value, n.value, st.value
+
+    # -- diagnostics, snapshots, timing ----------------------------------
+    def stats(self) -> dict:
+        s = abi.gg_stats_t()
+        _check(lib().gg_stats(self._h, C.byref(s)))
+        out = {k: getattr(s, k) for k, _ in abi.gg_stats_t._fields_}
+        for k in ("momentum", "center_of_mass"):
+            out[k] = tuple(out[k])
+        return out
+
+    def save(self, path: str):
+        _check(lib().gg_save(self._h, path.encode()))
+
+    def load(self, path: str):
+        _check(lib().gg_load(self._h, path.encode()))
+
+    def set_frame_timing(self, enabled: bool = True):
+        _check(lib().gg_set_frame_timing(self._h, int(bool(enabled))))
+
+    def get_frame_times(self):
+        n = C.c_int64()
+        _check(lib().gg_frame_times(self._h, None, 0, C.byref(n)))
+        out = np.zeros(max(n.value, 1), np.float32)
+        _check(lib().gg_frame_times(self._h, _fptr(out), out.shape[0], C.byref(n)))
+        return out[:n.value]
+
+    def profile_begin(self):
+        _check(lib().gg_profile_begin(self._h))
+
+    def profile_end(self) -> dict:
+        p = abi.gg_profile_t()
+        _check(lib().gg_profile_end(self._h, C.byref(p)))
+        out = {}
+        for k in range(p.n_classes):
+            name = bytes(p.names[k]).split(b"\0")[0].decode()
+            out[name] = {"launches": p.launches[k], "ms": p.ms[k], "units": p.units[k]}
+        return out
+
+    @property
+    def stream(self) -> int:
+        s = C.c_void_p()
+        _check(lib().gg_stream(self._h, C.byref(s)))
+        return s.value or 0
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().gg_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def scene_build(json_path: str, base_dir: str = None) -> dict:
+    """The particle sets and constructor arguments of a scene file, built on
+    the host (init_granular_system, main.cu:746-1173)."""
+    l = lib()
+    np_, nb, nu = C.c_int64(), C.c_int64(), C.c_int64()
+    bd = base_dir.encode() if base_dir else None
+    _check(l.gg_scene_build(json_path.encode(), bd, None, C.byref(np_), None, None, C.byref(nb), None,
+                            C.byref(nu), None))
+    p = np.zeros((max(np_.value, 1), 3), np.float32)
+    b = np.zeros((max(nb.value, 1), 3), np.float32)
+    a = np.zeros(max(nb.value, 1), np.int32)
+    u = np.zeros((max(nu.value, 1), 3), np.float32)
+    d = abi.gg_desc()
+    _check(l.gg_scene_build(json_path.encode(), bd, _fptr(p), C.byref(np_), _fptr(b), _iptr(a), C.byref(nb),
+                            _fptr(u), C.byref(nu), C.byref(d)))
+    return {
+        "particles": p[:np_.value], "boundary": b[:nb.value], "boundary_animated": a[:nb.value],
+        "upsampled": u[:nu.value], "space_size": tuple(d.space_size), "cell_length": d.cell_length,
+        "dt": d.dt, "gravity": tuple(d.gravity), "cell_size": tuple(d.cell_size), "density": d.density,
+        "upsampled_radius": d.upsampled_radius, "is_move_boundary": d.is_move_boundary,
+        "is_adaptive": d.is_adaptive, "params": d.params,
+    }
+
+
+class Grid:
+    """Stand-alone grid build (keys, stable sort, cell ranges) on the GPU."""
+
+    def __init__(self, capacity: int, cell_size, cell_length: float, device: int = 0):
+        self._h = None
+        cs = (C.c_int32 * 3)(*[int(x) for x in cell_size])
+        h = C.c_void_p()
+        _check(lib().gg_grid_create(int(device), int(capacity), cs, float(cell_length), C.byref(h)))
+        self._h = h
+        self.cell_size = tuple(int(x) for x in cell_size)
+
+    def build(self, pos):
+        p = _f32(pos)
+        n = p.shape[0]
+        ncell = self.cell_size[0] * self.cell_size[1] * self.cell_size[2]
+        keys = np.zeros(max(n, 1), np.int32)
+        sk = np.zeros(max(n, 1), np.int32)
+        perm = np.zeros(max(n, 1), np.int32)
+        cs = np.zeros(ncell + 1, np.int32)
+        _check(lib().gg_grid_build(self._h, _fptr(p), n, _iptr(keys), _iptr(sk), _iptr(perm), _iptr(cs)))
+        return keys[:n], sk[:n], perm[:n], cs
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().gg_grid_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,105 @@
+// common.cuh — device helpers shared by the kernels.
+//
+// Arithmetic here follows the reference's expressions operation by
+// operation (helper_math.h semantics for float3), and the library is built
+// with -fmad=false so no multiply-add is fused behind the source's back:
+// the CPU oracle (built with -ffp-contract=off) performs the same roundings.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "gg_internal.h"
+
+namespace gg {
+
+#define GG_PI_D 3.14159265358979323846
+#define GG_PI_F 3.14159265358979323846f
+
+__device__ __forceinline__ float3 f3(float4 a) { return make_float3(a.x, a.y, a.z); }
+__device__ __forceinline__ float3 add3(float3 a, float3 b) { return make_float3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ float3 sub3(float3 a, float3 b) { return make_float3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ float3 smul3(float s, float3 a) { return make_float3(s * a.x, s * a.y, s * a.z); }
+__device__ __forceinline__ float3 mul3s(float3 a, float s) { return make_float3(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ float3 div3s(float3 a, float s) { return make_float3(a.x / s, a.y / s, a.z / s); }
+// helper_math dot, left to right.
+__device__ __forceinline__ float dot3(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ float len3(float3 a) { return sqrtf(dot3(a, a)); }
+// helper_math normalize: v * rsqrtf(dot(v, v)).
+__device__ __forceinline__ float3 normalize3(float3 a) { return mul3s(a, rsqrtf(dot3(a, a))); }
+
+// particlePos2cellIdx, CUDAFunctions.cuh:71-79.
+__device__ __forceinline__ int cell_key(const Grid& g, int x, int y, int z) {
+  return (x >= 0 && x < g.nx && y >= 0 && y < g.ny && z >= 0 && z < g.nz)
+             ? ((x * g.ny) + y) * g.nz + z
+             : g.C;
+}
+
+// make_int3(pos / cell_length): IEEE division then truncation (cvt.rzi).
+__device__ __forceinline__ int3 trunc_cell(const Grid& g, float3 p) {
+  return make_int3(__float2int_rz(p.x / g.L), __float2int_rz(p.y / g.L), __float2int_rz(p.z / g.L));
+}
+// make_int3(floorf(pos / cell_length)).
+__device__ __forceinline__ int3 floor_cell(const Grid& g, float3 p) {
+  return make_int3(__float2int_rz(floorf(p.x / g.L)), __float2int_rz(floorf(p.y / g.L)),
+                   __float2int_rz(floorf(p.z / g.L)));
+}
+
+// Transcendentals by math mode: MM = 0 calls CUDA's float functions (the
+// ones the reference calls); MM = 1 evaluates in double and rounds once,
+// which the CPU restatement reproduces bit for bit.
+template <int MM> __device__ __forceinline__ float m_cbrt(float x) { return MM ? (float)cbrt((double)x) : cbrtf(x); }
+template <int MM> __device__ __forceinline__ float m_exp(float x) { return MM ? (float)exp((double)x) : expf(x); }
+template <int MM> __device__ __forceinline__ float m_acos(float x) { return MM ? (float)acos((double)x) : acosf(x); }
+template <int MM> __device__ __forceinline__ float m_rsqrt(float x) {
+  return MM ? (float)(1.0 / sqrt((double)x)) : rsqrtf(x);
+}
+template <int MM> __device__ __forceinline__ float m_norm3(float a, float b, float c) {
+  if (MM) {
+    const double da = a, db = b, dc = c;
+    return (float)sqrt(da * da + db * db + dc * dc);
+  }
+  return norm3df(a, b, c);
+}
+template <int MM> __device__ __forceinline__ float3 m_normalize3(float3 a) { return mul3s(a, m_rsqrt<MM>(dot3(a, a))); }
+
+// Radius laws, each exactly as the reference writes it.
+// compute_delta_pos passes `const int density` and uses double pi
+// (Solver.cu:28,311,320-321): cbrtf((3*m) / (4*pi*density)).
+template <int MM = 0>
+__device__ __forceinline__ float radius_contact(float m, int rho_i) {
+  return m_cbrt<MM>((float)((double)(3.0f * m) / (4.0 * GG_PI_D * (double)rho_i)));
+}
+// find_cover_vector / find_surface use float density, double PI_d
+// (GranularSystem.cu:28,518).
+template <int MM = 0>
+__device__ __forceinline__ float radius_surface(float m, float rho_f) {
+  return m_cbrt<MM>((float)((double)(3.0f * m) / (4.0 * GG_PI_D * (double)rho_f)));
+}
+// split_gpu: all float with the PI macro (Solver.cu:799).
+template <int MM = 0>
+__device__ __forceinline__ float radius_split(float m, float rho_f) {
+  return m_cbrt<MM>((3.0f * m) / ((4.0f * GG_PI_F) * rho_f));
+}
+
+__device__ __forceinline__ unsigned int fbits_abs_max(float a, float b) {
+  return __float_as_uint(fmaxf(fabsf(a), fabsf(b)));
+}
+
+// Warp-aggregated atomicMax of a non-negative float stored as bits.  NaN
+// bits compare above every finite value, so a NaN disables pruning.
+__device__ __forceinline__ void warp_max_bits(unsigned int* dst, unsigned int v) {
+  for (int o = 16; o > 0; o >>= 1) {
+    unsigned int w = __shfl_xor_sync(0xffffffffu, v, o);
+    v = v > w ? v : w;
+  }
+  if ((threadIdx.x & 31) == 0) atomicMax(dst, v);
+}
+
+__device__ __forceinline__ unsigned int lanemask_lt() {
+  unsigned int m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+}  // namespace gg

@@ -1,0 +1,238 @@
+// gg_internal.h — state of one gg_system and the kernel launchers shared by
+// the translation units of libgg.so.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/gg.h"
+
+namespace gg {
+
+// Grid geometry shared by every kernel: cell length and dims.
+struct Grid {
+  float L;
+  int nx, ny, nz;
+  int C;  // nx*ny*nz; the out-of-grid key
+};
+
+// Scalars that live on the device so a substep needs no host round trip.
+struct DevScalars {
+  unsigned int rmax_bits;      // max contact radius (float bits), this step
+  unsigned int inc_bits[64];   // per sweep: max |x* increment| (float bits)
+  unsigned int disp0_bits;     // max |dt v| of the predict (float bits)
+  int error_word;              // bit0 capacity, bit1 numeric
+  int n_after;                 // particle count after the adaptive step
+  int n_removed;
+  int n_split;
+  int n_split_appended;
+  int n_kept;
+};
+
+enum ErrorBits { ERR_CAPACITY = 1, ERR_NUMERIC = 2, ERR_TIMEOUT = 4 };
+
+// Kernel classes timed by gg_profile_*.
+enum ProfClass {
+  PC_HASH = 0, PC_SORT, PC_REORDER, PC_CELLSTART, PC_PREDICT, PC_SWEEP, PC_APPLY,
+  PC_FINALIZE, PC_UPSAMPLE, PC_UP_GRID, PC_SURFACE, PC_SURFDIST, PC_MERGE, PC_SPLIT,
+  PC_COMPACT, PC_STATS, PC_COUNT
+};
+
+// Double-buffered particle SoA; index `cur` is the live copy.
+struct Granular {
+  float4* pos[2] = {nullptr, nullptr};    // x, y, z, contact radius
+  float4* vel[2] = {nullptr, nullptr};    // x, y, z, unused
+  float* mass[2] = {nullptr, nullptr};
+  float* rs[2] = {nullptr, nullptr};      // surface-law radius
+  int32_t* units[2] = {nullptr, nullptr}; // integer mass ledger
+  float* merge[2] = {nullptr, nullptr};
+  int32_t* merge_units[2] = {nullptr, nullptr};
+  int32_t* merge_count[2] = {nullptr, nullptr};
+  int32_t* remove[2] = {nullptr, nullptr};
+  int32_t* als[2] = {nullptr, nullptr};   // adaptive_last_step (never permuted by the sort)
+  int cur = 0;
+  // never permuted or compacted (as in the reference)
+  float4* merge_vel = nullptr;
+  // recomputed every step
+  int32_t* surface = nullptr;
+  float* sdist = nullptr;
+  float4* cover = nullptr;
+  float4* xs = nullptr;       // predicted positions x*, w = contact radius
+  float* inv_m = nullptr;     // 1 / (m exp(-y))
+  float4* delta = nullptr;    // sweep output: dx, dy, dz, packed counts
+  int32_t* s_extra = nullptr; // reverse constraint counts delivered by atomics
+  int32_t* contacts = nullptr;
+  int32_t* ncon = nullptr;
+  // grid
+  uint32_t* keys = nullptr;   // sorted keys of the last build
+  uint32_t* perm = nullptr;   // sort permutation of the last build
+  int32_t* cell_start = nullptr;
+  // adaptive scratch
+  int32_t* prop = nullptr;
+  float* ldens = nullptr;
+  int32_t* winner = nullptr;
+  int32_t* split_flag = nullptr;
+  int32_t* keep_flag = nullptr;
+  int32_t* split_slot = nullptr;
+  int32_t* keep_slot = nullptr;
+  float4* child_pos = nullptr;
+};
+
+struct Boundary {
+  float4* pos = nullptr;        // live copy
+  int32_t* animated = nullptr;
+  float4* pos_alt = nullptr;    // reorder target, swapped with the live copy
+  int32_t* animated_alt = nullptr;
+  uint32_t* keys = nullptr;     // sorted keys of the last build
+  uint32_t* perm = nullptr;
+  int32_t* cell_start = nullptr;
+};
+
+struct Upsampled {
+  float4* pos[2] = {nullptr, nullptr};
+  float4* vel[2] = {nullptr, nullptr};
+  uint32_t* keys = nullptr;     // sorted keys of the last build
+  uint32_t* perm = nullptr;
+  int cur = 0;
+};
+
+// Scratch for the radix sort and scans, sized for max(cap, nu, nb, C+1).
+struct SortScratch {
+  uint32_t* k[2] = {nullptr, nullptr};
+  uint32_t* v[2] = {nullptr, nullptr};
+  uint32_t* hist = nullptr;   // 256 x tiles
+  int32_t* scan_blocks = nullptr;
+  int64_t capacity = 0;
+  int64_t hist_entries = 0;
+  int64_t scan_block_entries = 0;
+  int64_t* counter = nullptr;  // kernel launches are added here when set
+};
+
+struct Physics {
+  float dt;
+  float3 g;
+  float density;
+  int rho_i;
+  float space[3];
+  float upsampled_radius;
+  int is_move_boundary;
+  int is_adaptive;
+};
+
+}  // namespace gg
+
+struct gg_system {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  gg::Grid grid{};
+  gg_params P{};
+  gg::Physics phys{};
+  int64_t n = 0, cap = 0, nb = 0, nu = 0;
+  int64_t n_grid = 0;  // granular count at the last grid build (length of keys/perm)
+  gg::Granular g;
+  gg::Boundary b;
+  gg::Upsampled u;
+  gg::SortScratch sort;
+  gg::DevScalars* scal = nullptr;      // device
+  gg::DevScalars* scal_host = nullptr; // pinned mirror
+  double* stats_partial = nullptr;     // device FP64 partials
+  int stats_blocks = 0;
+  int num_sms = 0;
+  int64_t steps = 0;
+  int64_t launches = 0;                // kernels launched since create
+  int merge_iter = 0;
+  int64_t merged_last = 0, split_last = 0, merged_total = 0, split_total = 0;
+  int32_t error_word = 0;
+  std::vector<int64_t> stats_rows;     // merged, split, total per adaptive step
+  // timing
+  bool frame_timing = false;
+  std::vector<float> frame_times;
+  cudaEvent_t frame_ev[2] = {nullptr, nullptr};
+  bool profiling = false;
+  struct ProfEv { cudaEvent_t a, b; int cls; int64_t units; };
+  std::vector<ProfEv> prof_pending;
+  std::vector<cudaEvent_t> prof_pool;
+  size_t prof_pool_used = 0;
+  double prof_ms[gg::PC_COUNT] = {};
+  int64_t prof_launches[gg::PC_COUNT] = {};
+  int64_t prof_units[gg::PC_COUNT] = {};
+};
+
+struct gg_grid {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  gg::Grid grid{};
+  int64_t cap = 0;
+  float4* pos = nullptr;
+  uint32_t* keys_unsorted = nullptr;
+  uint32_t* sorted_keys = nullptr;
+  uint32_t* perm = nullptr;
+  int32_t* cell_start = nullptr;
+  gg::SortScratch sort;
+};
+
+namespace gg {
+
+// ---- error handling (api.cpp) ----
+void set_error(const std::string& msg);
+gg_status cuda_status(cudaError_t e, const char* what);
+#define GG_CUDA(call)                                               \
+  do {                                                              \
+    cudaError_t e__ = (call);                                       \
+    if (e__ != cudaSuccess) return gg::cuda_status(e__, #call);     \
+  } while (0)
+
+// ---- launchers (kernels_*.cu) ----
+// grid
+gg_status sort_scratch_alloc(SortScratch& s, int64_t capacity);
+void sort_scratch_free(SortScratch& s);
+int key_bits(int C);
+// Computes keys of pos[0..n) and the stable sort permutation; sorted keys in
+// keys_out, permutation in perm_out (both device, n entries).
+gg_status grid_sort(const Grid& g, const float4* pos, int64_t n, SortScratch& s,
+                    uint32_t* keys_out, uint32_t* perm_out, uint32_t* keys_unsorted_out,
+                    cudaStream_t st, gg_system* prof);
+gg_status cell_start_build(const Grid& g, const uint32_t* sorted_keys, int64_t n,
+                           int32_t* cell_start, SortScratch& s, cudaStream_t st, gg_system* prof);
+gg_status exclusive_scan(const int32_t* in, int32_t* out, int64_t n, SortScratch& s,
+                         cudaStream_t st, int32_t* total_out_dev);
+gg_status reorder_granular(gg_system* S, cudaStream_t st);
+gg_status reorder_boundary(gg_system* S, const uint32_t* perm, cudaStream_t st);
+gg_status reorder_upsampled(gg_system* S, const uint32_t* perm, cudaStream_t st);
+
+// solve
+gg_status radii_all(gg_system* S, cudaStream_t st);
+gg_status predict(gg_system* S, cudaStream_t st);
+gg_status sweep(gg_system* S, int it, cudaStream_t st);
+gg_status apply(gg_system* S, int it, bool stab, bool last, cudaStream_t st);
+gg_status finalize(gg_system* S, cudaStream_t st);
+gg_status upsample(gg_system* S, cudaStream_t st);
+gg_status explosion(gg_system* S, float force, cudaStream_t st);
+
+// adaptive
+gg_status surface(gg_system* S, cudaStream_t st);
+gg_status surface_distance(gg_system* S, cudaStream_t st);
+gg_status merge_mark(gg_system* S, cudaStream_t st);
+gg_status merge_count(gg_system* S, cudaStream_t st);
+gg_status split_and_compact(gg_system* S, cudaStream_t st);
+
+// stats
+gg_status stats_compute(gg_system* S, gg_stats_t* out);
+
+// profiling hooks (system.cu)
+void prof_begin(gg_system* S, int cls, cudaStream_t st);
+void prof_end(gg_system* S, int cls, int64_t units, cudaStream_t st);
+
+inline int blocks_for(int64_t n, int threads) {
+  return (int)((n + threads - 1) / threads);
+}
+
+inline void count_launches(gg_system* S, int k) {
+  if (S) S->launches += k;
+}
+
+}  // namespace gg

@@ -1,0 +1,528 @@
+// kernels_adapt.cu — surface detection, distance to the surface, adaptive
+// merge/split and the compaction that follows.
+//
+// Replaces GranularSystem::set_surface_particles / find_distance_to_surface
+// (GranularSystem.cu:506-699) and Solver::adaptive_sampling with
+// merge_mark_gpu, merge_count_gpu, split_gpu and the DArray compactions and
+// appends (Solver.cu:526-1242, DArray.hpp:62-155).  No allocation and no
+// host round trip except the new particle count.
+#include "common.cuh"
+
+namespace gg {
+
+// ------------------------------------------------------------ surface
+
+// find_cover_vector + find_surface (GranularSystem.cu:506-611) fused: the
+// cover vector of i is only needed by i, so one thread makes both passes.
+template <int MM>
+__global__ void __launch_bounds__(256) k_surface(Grid g, int n, const float4* __restrict__ pos,
+                                                 const float* __restrict__ rs, const int32_t* __restrict__ cs,
+                                                 int32_t* __restrict__ surface, float cone, int min_nb) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float3 xi = f3(pos[i]);
+  const float ri = rs[i];
+  const int3 q = trunc_cell(g, xi);
+  float3 cv = make_float3(0.f, 0.f, 0.f);
+  for (int m = 0; m < 27; ++m) {
+    const int cell = cell_key(g, q.x + m / 9 - 1, q.y + (m % 9) / 3 - 1, q.z + m % 3 - 1);
+    if (cell == g.C) continue;
+    const int j1 = cs[cell + 1];
+    for (int j = cs[cell]; j < j1; ++j) {
+      if (j == i) continue;
+      const float3 d = sub3(xi, f3(pos[j]));
+      const float dis = len3(d);
+      if (dis > 2.0f * (ri + rs[j])) continue;
+      cv = add3(cv, m_normalize3<MM>(d));
+    }
+  }
+  const float3 c = m_normalize3<MM>(cv);
+  bool vote = false;
+  unsigned nn = 0;
+  for (int m = 0; m < 27; ++m) {
+    const int cell = cell_key(g, q.x + m / 9 - 1, q.y + (m % 9) / 3 - 1, q.z + m % 3 - 1);
+    if (cell == g.C) continue;
+    const int j1 = cs[cell + 1];
+    for (int j = cs[cell]; j < j1; ++j) {
+      if (j == i) continue;
+      float3 b = sub3(f3(pos[j]), xi);
+      const float dis = len3(b);
+      if (dis > 2.0f * (ri + rs[j])) continue;
+      b = m_normalize3<MM>(b);
+      if (m_acos<MM>(dot3(b, c)) <= cone) vote = true;
+      ++nn;
+    }
+  }
+  surface[i] = (nn <= (unsigned)min_nb || !vote) ? 1 : 0;
+}
+
+gg_status surface(gg_system* S, cudaStream_t st) {
+  if (S->n <= 0) return GG_OK;
+  const int c = S->g.cur;
+  prof_begin(S, PC_SURFACE, st);
+  auto kern = S->P.math_mode ? k_surface<1> : k_surface<0>;
+  kern<<<blocks_for(S->n, 256), 256, 0, st>>>(S->grid, (int)S->n, S->g.pos[c], S->g.rs[c], S->g.cell_start,
+                                                   S->g.surface, S->P.surface_cone, S->P.surface_min_neighbors);
+  count_launches(S, 1);
+  prof_end(S, PC_SURFACE, S->n, st);
+  GG_CUDA(cudaGetLastError());
+  return GG_OK;
+}
+
+// compute_distance_to_surface, GranularSystem.cu:639-688.
+__global__ void __launch_bounds__(256) k_surfdist(Grid g, int n, const float4* __restrict__ pos,
+                                                  const int32_t* __restrict__ surface,
+                                                  const int32_t* __restrict__ cs, float* __restrict__ sdist,
+                                                  float none) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (surface[i] == 1) {
+    sdist[i] = 0.0f;
+    return;
+  }
+  const float3 xi = f3(pos[i]);
+  const int3 q = trunc_cell(g, xi);
+  float best = none;
+  for (int m = 0; m < 27; ++m) {
+    const int cell = cell_key(g, q.x + m / 9 - 1, q.y + (m % 9) / 3 - 1, q.z + m % 3 - 1);
+    if (cell == g.C) continue;
+    const int j1 = cs[cell + 1];
+    for (int j = cs[cell]; j < j1; ++j) {
+      if (j == i || surface[j] == 0) continue;
+      const float3 d = sub3(xi, f3(pos[j]));
+      const float d2 = dot3(d, d);
+      if (d2 < best) best = d2;
+    }
+  }
+  sdist[i] = best;
+}
+
+gg_status surface_distance(gg_system* S, cudaStream_t st) {
+  if (S->n <= 0) return GG_OK;
+  prof_begin(S, PC_SURFDIST, st);
+  k_surfdist<<<blocks_for(S->n, 256), 256, 0, st>>>(S->grid, (int)S->n, S->g.pos[S->g.cur], S->g.surface,
+                                                    S->g.cell_start, S->g.sdist, S->P.no_surface_distance);
+  count_launches(S, 1);
+  prof_end(S, PC_SURFDIST, S->n, st);
+  GG_CUDA(cudaGetLastError());
+  return GG_OK;
+}
+
+// ------------------------------------------------------------ merge
+
+struct MergeArgs {
+  Grid g;
+  int n;
+  const float4* __restrict__ pos;
+  const float4* __restrict__ vel;
+  const float* __restrict__ mass;
+  const int32_t* __restrict__ units;
+  const int32_t* __restrict__ surface;
+  const float* __restrict__ sdist;
+  const int32_t* __restrict__ cs;
+  int32_t* __restrict__ remove;
+  float* __restrict__ merge;
+  int32_t* __restrict__ merge_units;
+  float4* __restrict__ merge_vel;
+  int32_t* __restrict__ prop;
+  float* __restrict__ ldens;
+  int32_t* __restrict__ winner;
+  float max_mass, min_mass, sdt, target_density;
+  double merge_radius;
+  float merge_radius_f;  // smallest float above merge_radius: dis < r (double) <=> dis < this
+};
+
+// merge_mark_gpu (Solver.cu:526-653), scan phase: every thread's neighbour
+// scan sees remove[] as it was at kernel start.
+__global__ void __launch_bounds__(256) k_merge_scan(MergeArgs a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  a.winner[i] = 0x7fffffff;
+  a.prop[i] = -1;
+  const float mi = a.mass[i];
+  if (a.surface[i] != 0 || a.remove[i] != 0 || mi < a.min_mass || mi >= a.max_mass || a.sdist[i] < a.sdt) return;
+  const float3 xi = f3(a.pos[i]);
+  const int3 q = trunc_cell(a.g, xi);
+  float closest = 1000.0f;
+  int ci = -1;
+  float ld = 0.0f;
+  int lc = 0;
+  for (int m = 0; m < 27; ++m) {
+    const int cell = cell_key(a.g, q.x + m / 9 - 1, q.y + (m % 9) / 3 - 1, q.z + m % 3 - 1);
+    if (cell == a.g.C) continue;
+    const int j1 = a.cs[cell + 1];
+    for (int j = a.cs[cell]; j < j1 && j < a.n; ++j) {
+      const float dis = len3(sub3(xi, f3(a.pos[j])));
+      const bool inr = dis < a.merge_radius_f;
+      if (inr) {
+        ld += a.mass[j];
+        ++lc;
+      }
+      if (j <= i || a.remove[j] != 0 || a.surface[j] != 0 || a.sdist[i] < a.sdt) continue;
+      if (mi + a.mass[j] > a.max_mass) continue;
+      if (inr && dis < closest) {
+        closest = dis;
+        ci = j;
+      }
+    }
+  }
+  if (lc > 0 && ci != -1) {
+    a.prop[i] = ci;
+    a.ldens[i] = ld / (float)lc;
+  }
+}
+
+__device__ __forceinline__ bool outer_ok(const MergeArgs& a, int i) {
+  return a.surface[i] == 0 && a.sdist[i] > a.sdt;
+}
+
+// Second-CAS order: ascending proposer index, so the lowest proposer of a
+// target that is not itself a proposer wins it.
+__global__ void k_merge_winner(MergeArgs a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  const int t = a.prop[i];
+  if (t < 0 || !outer_ok(a, i) || a.prop[t] >= 0) return;
+  atomicMin(&a.winner[t], i);
+}
+
+// The compare-and-swap stages of merge_mark_gpu (Solver.cu:608-651) under
+// the phase-ordered schedule: every proposer first wins its own CAS; then
+// the second CASes run in ascending index.
+__global__ void k_merge_apply(MergeArgs a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  const int t = a.prop[i];
+  if (t < 0) return;
+  a.remove[i] = -1;
+  if (!outer_ok(a, i)) return;
+  if (a.prop[t] >= 0 || a.winner[t] != i) {
+    a.remove[i] = 0;
+    return;
+  }
+  a.remove[t] = -1;
+  if (!outer_ok(a, t)) {
+    a.remove[i] = 0;
+    return;
+  }
+  const float mi = a.mass[i], mt = a.mass[t];
+  a.merge[t] = mi;
+  a.merge[i] = -mi;
+  a.merge_units[t] = a.units[i];
+  a.merge_units[i] = -a.units[i];
+  const float m_t = 1.0f / (mi + mt);
+  const float3 vt = smul3(m_t, add3(smul3(mi, f3(a.vel[i])), smul3(mt, f3(a.vel[t]))));
+  a.merge_vel[i] = make_float4(-vt.x, -vt.y, -vt.z, 0.f);
+  const float df = fminf(1.0f, a.ldens[i] / a.target_density);
+  const float3 mv = mul3s(vt, 1.0f + (1.0f - df) * 0.1f);
+  a.merge_vel[t] = make_float4(mv.x, mv.y, mv.z, 0.f);
+}
+
+gg_status merge_mark(gg_system* S, cudaStream_t st) {
+  if (S->n <= 0) return GG_OK;
+  const int c = S->g.cur;
+  MergeArgs a;
+  a.g = S->grid;
+  a.n = (int)S->n;
+  a.pos = S->g.pos[c];
+  a.vel = S->g.vel[c];
+  a.mass = S->g.mass[c];
+  a.units = S->g.units[c];
+  a.surface = S->g.surface;
+  a.sdist = S->g.sdist;
+  a.cs = S->g.cell_start;
+  a.remove = S->g.remove[c];
+  a.merge = S->g.merge[c];
+  a.merge_units = S->g.merge_units[c];
+  a.merge_vel = S->g.merge_vel;
+  a.prop = S->g.prop;
+  a.ldens = S->g.ldens;
+  a.winner = S->g.winner;
+  a.max_mass = S->P.max_mass;
+  a.min_mass = S->P.min_merge_mass;
+  a.sdt = S->P.surface_dist_threshold;
+  a.target_density = S->P.target_density;
+  a.merge_radius = S->P.merge_radius;
+  {
+    // float threshold equivalent to the double comparison dis < merge_radius
+    float f = (float)S->P.merge_radius;
+    if ((double)f < S->P.merge_radius) f = nextafterf(f, INFINITY);
+    a.merge_radius_f = f;
+    // dis < r_d  <=>  dis < f when f is the smallest float >= r_d and f != r_d;
+    // when f == r_d exactly the comparison is already exact.
+  }
+  const int nb = blocks_for(S->n, 256);
+  prof_begin(S, PC_MERGE, st);
+  k_merge_scan<<<nb, 256, 0, st>>>(a);
+  k_merge_winner<<<nb, 256, 0, st>>>(a);
+  k_merge_apply<<<nb, 256, 0, st>>>(a);
+  count_launches(S, 3);
+  prof_end(S, PC_MERGE, S->n, st);
+  GG_CUDA(cudaGetLastError());
+  return GG_OK;
+}
+
+// merge_count_gpu (Solver.cu:658-699).  With the integer ledger the transfer
+// of blend step k is floor(M(k+1)/B) - floor(Mk/B) units, so the B
+// transfers sum to M exactly.  Radii follow the new mass.
+template <int MM>
+__global__ void k_merge_count(int n, float4* __restrict__ pos, float4* __restrict__ vel,
+                              float* __restrict__ mass, float* __restrict__ rs, int32_t* __restrict__ units,
+                              float* __restrict__ merge, int32_t* __restrict__ merge_units,
+                              int32_t* __restrict__ merge_count, int32_t* __restrict__ remove,
+                              int32_t* __restrict__ als, const float4* __restrict__ merge_vel, int B,
+                              int ledger, int rho_i, float rho_f) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (remove[i] != -1) return;
+  const int old = merge_count[i];
+  merge_count[i] = old + 1;
+  const float4 mv = merge_vel[i];
+  const float3 dvel = div3s(make_float3(mv.x, mv.y, mv.z), (float)B);
+  float m;
+  if (ledger) {
+    const int mu = merge_units[i];
+    const long long M = mu < 0 ? -(long long)mu : (long long)mu;
+    long long amt = (M * (old + 1)) / B - (M * old) / B;
+    if (mu < 0) amt = -amt;
+    units[i] = units[i] + (int)amt;
+    m = (float)((double)units[i] / (double)(1 << 20));
+  } else {
+    const float delta = merge[i] / (float)B;
+    m = mass[i] + delta;
+  }
+  mass[i] = m;
+  als[i] = 1;
+  float4 v = vel[i];
+  v.x = v.x + dvel.x;
+  v.y = v.y + dvel.y;
+  v.z = v.z + dvel.z;
+  vel[i] = v;
+  pos[i].w = radius_contact<MM>(m, rho_i);
+  rs[i] = radius_surface<MM>(m, rho_f);
+  if (old + 1 == B) {
+    const bool giver = ledger ? (merge_units[i] < 0) : (merge[i] < 0.0f);
+    if (giver) {
+      remove[i] = 1;
+      als[i] = 0;
+    } else {
+      remove[i] = 0;
+    }
+    merge_count[i] = 0;
+    merge[i] = 0.0f;
+    merge_units[i] = 0;
+  }
+}
+
+gg_status merge_count(gg_system* S, cudaStream_t st) {
+  if (S->n <= 0) return GG_OK;
+  const int c = S->g.cur;
+  prof_begin(S, PC_MERGE, st);
+  auto kern = S->P.math_mode ? k_merge_count<1> : k_merge_count<0>;
+  kern<<<blocks_for(S->n, 256), 256, 0, st>>>(
+      (int)S->n, S->g.pos[c], S->g.vel[c], S->g.mass[c], S->g.rs[c], S->g.units[c], S->g.merge[c],
+      S->g.merge_units[c], S->g.merge_count[c], S->g.remove[c], S->g.als[c], S->g.merge_vel, S->P.blend_factor,
+      S->P.mass_ledger, S->phys.rho_i, S->phys.density);
+  count_launches(S, 1);
+  prof_end(S, PC_MERGE, S->n, st);
+  GG_CUDA(cudaGetLastError());
+  return GG_OK;
+}
+
+// ------------------------------------------------------------ split
+
+// split_gpu + check_neighborhood (Solver.cu:708-827): decides which surface
+// particles split and where the child goes.  Also the keep flags of the
+// compaction (remove == 1 is dropped, DArray.hpp:79-90).
+template <int MM>
+__global__ void __launch_bounds__(256) k_split_mark(Grid g, int n, const float4* __restrict__ pos,
+                                                    const float* __restrict__ mass,
+                                                    const int32_t* __restrict__ surface,
+                                                    const int32_t* __restrict__ remove,
+                                                    const int32_t* __restrict__ cs, const int32_t* __restrict__ bcs,
+                                                    const float4* __restrict__ bpos, float split_min, float rho_f,
+                                                    int32_t* __restrict__ split_flag, int32_t* __restrict__ keep,
+                                                    float4* __restrict__ child_pos) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  keep[i] = remove[i] != 1;
+  split_flag[i] = 0;
+  const float mi = mass[i];
+  if (remove[i] != 0 || surface[i] != 1 || mi <= split_min) return;
+  const float r_i = radius_split<MM>(mi, rho_f);
+  const float max_dist = 2.0f * r_i;
+  const float3 p = f3(pos[i]);
+  const int3 q = trunc_cell(g, p);
+  bool found = false;
+  float3 center = make_float3(0.f, 0.f, 0.f);
+  for (int m = 0; m < 27; ++m) {
+    const int cx = q.x + m / 9 - 1, cy = q.y + (m % 9) / 3 - 1, cz = q.z + m % 3 - 1;
+    const int cell = cell_key(g, cx, cy, cz);
+    if (cell == g.C) continue;
+    if (!found && m != 13) {
+      if (cs[cell] == cs[cell + 1] && bcs[cell] == bcs[cell + 1]) {
+        center = make_float3(((float)cx + 0.5f) * g.L, ((float)cy + 0.5f) * g.L, ((float)cz + 0.5f) * g.L);
+        found = true;
+      }
+    }
+    const int j1 = bcs[cell + 1];
+    for (int j = bcs[cell]; j < j1; ++j) {
+      if (len3(sub3(p, f3(bpos[j]))) < max_dist) return;
+    }
+  }
+  if (!found) return;
+  split_flag[i] = 1;
+  child_pos[i] = make_float4(center.x, center.y, center.z, 0.f);
+}
+
+struct CompactArgs {
+  int n;
+  int cap;
+  int ledger;
+  int rho_i;
+  float rho_f;
+  const int32_t* __restrict__ keep_slot;
+  const int32_t* __restrict__ split_slot;
+  const int32_t* __restrict__ split_flag;
+  const float4* __restrict__ child_pos;
+  const DevScalars* __restrict__ scal;
+  int* __restrict__ error_word;
+  // in
+  const float4* __restrict__ pos;
+  const float4* __restrict__ vel;
+  const float* __restrict__ mass;
+  const float* __restrict__ rs;
+  const int32_t* __restrict__ units;
+  const int32_t* __restrict__ als;
+  const int32_t* __restrict__ mc;
+  const float* __restrict__ merge;
+  const int32_t* __restrict__ mu;
+  const int32_t* __restrict__ remove;
+  // out
+  float4* __restrict__ pos_o;
+  float4* __restrict__ vel_o;
+  float* __restrict__ mass_o;
+  float* __restrict__ rs_o;
+  int32_t* __restrict__ units_o;
+  int32_t* __restrict__ als_o;
+  int32_t* __restrict__ mc_o;
+  float* __restrict__ merge_o;
+  int32_t* __restrict__ mu_o;
+  int32_t* __restrict__ remove_o;
+};
+
+// Stream compaction of every compacted SoA field (order kept) followed by
+// the children appended in ascending parent index (Solver.cu:1168-1221).
+// A split parent keeps half of its mass (Solver.cu:816-826).
+template <int MM>
+__global__ void k_compact(CompactArgs a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  if (a.remove[i] == 1) return;
+  const int d = a.keep_slot[i];
+  float4 p = a.pos[i];
+  float m = a.mass[i];
+  float r_s = a.rs[i];
+  int u = a.units[i];
+  int al = a.als[i];
+  if (a.split_flag[i]) {
+    float mc_child;
+    int uc = 0;
+    if (a.ledger) {
+      uc = u / 2;
+      u = u - uc;
+      m = (float)((double)u / (double)(1 << 20));
+      mc_child = (float)((double)uc / (double)(1 << 20));
+    } else {
+      const float h = m / 2.0f;
+      m = h;
+      mc_child = h;
+    }
+    p.w = radius_contact<MM>(m, a.rho_i);
+    r_s = radius_surface<MM>(m, a.rho_f);
+    al = 1;
+    const int cd = a.scal->n_kept + a.split_slot[i];
+    if (cd < a.cap) {
+      const float4 cp = a.child_pos[i];
+      a.pos_o[cd] = make_float4(cp.x, cp.y, cp.z, radius_contact<MM>(mc_child, a.rho_i));
+      a.vel_o[cd] = a.vel[i];
+      a.mass_o[cd] = mc_child;
+      a.rs_o[cd] = radius_surface<MM>(mc_child, a.rho_f);
+      a.units_o[cd] = uc;
+      a.als_o[cd] = 1;
+      a.mc_o[cd] = 0;
+      a.merge_o[cd] = 0.0f;
+      a.mu_o[cd] = 0;
+      a.remove_o[cd] = 0;
+    } else {
+      atomicOr(a.error_word, ERR_CAPACITY);
+    }
+  }
+  a.pos_o[d] = p;
+  a.vel_o[d] = a.vel[i];
+  a.mass_o[d] = m;
+  a.rs_o[d] = r_s;
+  a.units_o[d] = u;
+  a.als_o[d] = al;
+  a.mc_o[d] = a.mc[i];
+  a.merge_o[d] = a.merge[i];
+  a.mu_o[d] = a.mu[i];
+  a.remove_o[d] = a.remove[i];
+}
+
+__global__ void k_adapt_counts(DevScalars* s, int n, int cap) {
+  const int kept = s->n_kept;
+  const int split = s->n_split;
+  const int room = cap - kept;
+  const int app = split < room ? split : (room > 0 ? room : 0);
+  s->n_removed = n - kept;
+  s->n_split_appended = app;
+  s->n_after = kept + app;
+}
+
+gg_status split_and_compact(gg_system* S, cudaStream_t st) {
+  if (S->n <= 0) return GG_OK;
+  Granular& G = S->g;
+  const int c = G.cur, o = c ^ 1;
+  const int nb = blocks_for(S->n, 256);
+  prof_begin(S, PC_SPLIT, st);
+  auto kmark = S->P.math_mode ? k_split_mark<1> : k_split_mark<0>;
+  kmark<<<nb, 256, 0, st>>>(S->grid, (int)S->n, G.pos[c], G.mass[c], G.surface, G.remove[c], G.cell_start,
+                                   S->b.cell_start, S->b.pos, S->P.split_min_mass, S->phys.density, G.split_flag,
+                                   G.keep_flag, G.child_pos);
+  count_launches(S, 1);
+  prof_end(S, PC_SPLIT, S->n, st);
+  prof_begin(S, PC_COMPACT, st);
+  gg_status rc = exclusive_scan(G.keep_flag, G.keep_slot, S->n, S->sort, st, &S->scal->n_kept);
+  if (rc != GG_OK) return rc;
+  rc = exclusive_scan(G.split_flag, G.split_slot, S->n, S->sort, st, &S->scal->n_split);
+  if (rc != GG_OK) return rc;
+  CompactArgs a;
+  a.n = (int)S->n;
+  a.cap = (int)S->cap;
+  a.ledger = S->P.mass_ledger;
+  a.rho_i = S->phys.rho_i;
+  a.rho_f = S->phys.density;
+  a.keep_slot = G.keep_slot;
+  a.split_slot = G.split_slot;
+  a.split_flag = G.split_flag;
+  a.child_pos = G.child_pos;
+  a.scal = S->scal;
+  a.error_word = &S->scal->error_word;
+  a.pos = G.pos[c]; a.vel = G.vel[c]; a.mass = G.mass[c]; a.rs = G.rs[c]; a.units = G.units[c];
+  a.als = G.als[c]; a.mc = G.merge_count[c]; a.merge = G.merge[c]; a.mu = G.merge_units[c];
+  a.remove = G.remove[c];
+  a.pos_o = G.pos[o]; a.vel_o = G.vel[o]; a.mass_o = G.mass[o]; a.rs_o = G.rs[o]; a.units_o = G.units[o];
+  a.als_o = G.als[o]; a.mc_o = G.merge_count[o]; a.merge_o = G.merge[o]; a.mu_o = G.merge_units[o];
+  a.remove_o = G.remove[o];
+  auto kcomp = S->P.math_mode ? k_compact<1> : k_compact<0>;
+  kcomp<<<nb, 256, 0, st>>>(a);
+  k_adapt_counts<<<1, 1, 0, st>>>(S->scal, (int)S->n, (int)S->cap);
+  count_launches(S, 2);
+  prof_end(S, PC_COMPACT, S->n, st);
+  G.cur = o;
+  GG_CUDA(cudaGetLastError());
+  return GG_OK;
+}
+
+}  // namespace gg

@@ -1,0 +1,390 @@
+// kernels_grid.cu — uniform-grid neighbour structure.
+//
+// Replaces neighbor_search_{granular,boundary,upsampled}
+// (GranularSystem.cu:65-395) and the primitives of CUDAFunctions.cuh:54-107:
+//   cell key per particle  -> stable LSD radix sort of (key, index)
+//   -> one gather of every SoA field -> cell_start by count + exclusive scan.
+// The sort is stable, as thrust::sort_by_key on int keys is, so the sorted
+// order is identical; it sorts only ceil(log2(C+1)) key bits.
+#include <utility>
+
+#include "common.cuh"
+
+namespace gg {
+
+constexpr int kSortThreads = 256;
+constexpr int kSortItems = 16;
+constexpr int kSortTile = kSortThreads * kSortItems;  // 4096
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 16;
+constexpr int kScanTile = kScanThreads * kScanItems;   // 4096
+constexpr int kScanTopThreads = 1024;
+constexpr int kScanTopItems = 16;
+constexpr int64_t kScanMaxBlocks = (int64_t)kScanTopThreads * kScanTopItems;
+
+int key_bits(int C) {
+  int b = 1;
+  while (b < 31 && ((int64_t)1 << b) <= (int64_t)C) ++b;
+  return b;  // keys take values 0..C
+}
+
+// ------------------------------------------------------------------ hash
+
+// mapParticles2Cells_CUDA (CUDAFunctions.cuh:91-107) with the sort's value
+// array (thrust::sequence, GranularSystem.cu:71-73) produced in one pass.
+__global__ void k_hash(Grid g, const float4* __restrict__ pos, int n, uint32_t* __restrict__ keys,
+                       uint32_t* __restrict__ vals, uint32_t* __restrict__ keys_copy) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4 p = pos[i];
+  const int3 c = floor_cell(g, make_float3(p.x, p.y, p.z));
+  const uint32_t k = (uint32_t)cell_key(g, c.x, c.y, c.z);
+  keys[i] = k;
+  vals[i] = (uint32_t)i;
+  if (keys_copy) keys_copy[i] = k;
+}
+
+// ------------------------------------------------------------ block scan
+
+// Exclusive scan of one int per thread across a block of kThreads threads;
+// returns the block total in *total.
+template <int kThreads>
+__device__ __forceinline__ int block_exclusive_scan(int v, int* total) {
+  __shared__ int warp_tot[kThreads / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) warp_tot[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    int w = lane < kThreads / 32 ? warp_tot[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    if (lane < kThreads / 32) warp_tot[lane] = w;
+  }
+  __syncthreads();
+  const int warp_prefix = warp ? warp_tot[warp - 1] : 0;
+  *total = warp_tot[kThreads / 32 - 1];
+  __syncthreads();
+  return warp_prefix + x - v;
+}
+
+// -------------------------------------------------------- exclusive scan
+
+__global__ void k_scan_reduce(const int32_t* __restrict__ in, int64_t n, int32_t* __restrict__ bsum) {
+  const int64_t base = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanItems;
+  int s = 0;
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    const int64_t i = base + k;
+    if (i < n) s += in[i];
+  }
+  int tot;
+  block_exclusive_scan<kScanThreads>(s, &tot);
+  if (threadIdx.x == 0) bsum[blockIdx.x] = tot;
+}
+
+__global__ void k_scan_top(int32_t* __restrict__ bsum, int nb, int32_t* __restrict__ total_out) {
+  const int base = threadIdx.x * kScanTopItems;
+  int v[kScanTopItems];
+  int s = 0;
+#pragma unroll
+  for (int k = 0; k < kScanTopItems; ++k) {
+    v[k] = (base + k < nb) ? bsum[base + k] : 0;
+    s += v[k];
+  }
+  int tot;
+  int run = block_exclusive_scan<kScanTopThreads>(s, &tot);
+#pragma unroll
+  for (int k = 0; k < kScanTopItems; ++k) {
+    if (base + k < nb) bsum[base + k] = run;
+    run += v[k];
+  }
+  if (threadIdx.x == 0 && total_out) *total_out = tot;
+}
+
+__global__ void k_scan_down(const int32_t* in, int32_t* out, int64_t n, const int32_t* __restrict__ bsum) {
+  const int64_t base = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanItems;
+  int v[kScanItems];
+  int s = 0;
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    const int64_t i = base + k;
+    v[k] = i < n ? in[i] : 0;
+    s += v[k];
+  }
+  int tot;
+  int run = block_exclusive_scan<kScanThreads>(s, &tot) + bsum[blockIdx.x];
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    const int64_t i = base + k;
+    if (i < n) out[i] = run;
+    run += v[k];
+  }
+}
+
+gg_status exclusive_scan(const int32_t* in, int32_t* out, int64_t n, SortScratch& s, cudaStream_t st,
+                         int32_t* total_out_dev) {
+  if (n <= 0) {
+    if (total_out_dev) GG_CUDA(cudaMemsetAsync(total_out_dev, 0, sizeof(int32_t), st));
+    return GG_OK;
+  }
+  const int64_t nb = (n + kScanTile - 1) / kScanTile;
+  if (nb > kScanMaxBlocks || nb > s.scan_block_entries) {
+    set_error("exclusive_scan: input larger than the scan scratch");
+    return GG_ERR_INVALID_ARGUMENT;
+  }
+  k_scan_reduce<<<(unsigned)nb, kScanThreads, 0, st>>>(in, n, s.scan_blocks);
+  k_scan_top<<<1, kScanTopThreads, 0, st>>>(s.scan_blocks, (int)nb, total_out_dev);
+  k_scan_down<<<(unsigned)nb, kScanThreads, 0, st>>>(in, out, n, s.scan_blocks);
+  if (s.counter) *s.counter += 3;
+  GG_CUDA(cudaGetLastError());
+  return GG_OK;
+}
+
+// ------------------------------------------------------------ radix sort
+
+// Per-tile histogram of one 8-bit digit; hist is digit-major [256][tiles].
+__global__ void k_radix_hist(const uint32_t* __restrict__ keys, int n, int shift, int tiles,
+                             uint32_t* __restrict__ hist) {
+  __shared__ uint32_t h[256];
+  h[threadIdx.x] = 0;
+  __syncthreads();
+  const int base = blockIdx.x * kSortTile;
+#pragma unroll 4
+  for (int r = 0; r < kSortItems; ++r) {
+    const int i = base + r * kSortThreads + threadIdx.x;
+    if (i < n) atomicAdd(&h[(keys[i] >> shift) & 255u], 1u);
+  }
+  __syncthreads();
+  hist[threadIdx.x * tiles + blockIdx.x] = h[threadIdx.x];
+}
+
+// Stable scatter: items are ranked in index order within the tile (rounds
+// of 256 consecutive items; within a round by warp, then by lane).
+__global__ void k_radix_scatter(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin,
+                                uint32_t* __restrict__ kout, uint32_t* __restrict__ vout, int n,
+                                int shift, int tiles, const uint32_t* __restrict__ offs) {
+  constexpr int W = kSortThreads / 32;
+  __shared__ uint32_t base_d[256];
+  __shared__ uint32_t wcnt[W][256];
+  const int t = threadIdx.x, warp = t >> 5;
+  base_d[t] = offs[t * tiles + blockIdx.x];
+  const int base = blockIdx.x * kSortTile;
+  const unsigned lt = lanemask_lt();
+  for (int r = 0; r < kSortItems; ++r) {
+#pragma unroll
+    for (int w = 0; w < W; ++w) wcnt[w][t] = 0;
+    __syncthreads();
+    const int i = base + r * kSortThreads + t;
+    const bool valid = i < n;
+    uint32_t k = 0, v = 0, d = 256;
+    if (valid) {
+      k = kin[i];
+      v = vin[i];
+      d = (k >> shift) & 255u;
+    }
+    const unsigned peers = __match_any_sync(0xffffffffu, d);
+    const int rank = __popc(peers & lt);
+    if (valid && rank == 0) wcnt[warp][d] = __popc(peers);
+    __syncthreads();
+    if (valid) {
+      uint32_t pre = 0;
+      for (int w = 0; w < warp; ++w) pre += wcnt[w][d];
+      const uint32_t dst = base_d[d] + pre + rank;
+      kout[dst] = k;
+      vout[dst] = v;
+    }
+    __syncthreads();
+    uint32_t tot = 0;
+#pragma unroll
+    for (int w = 0; w < W; ++w) tot += wcnt[w][t];
+    base_d[t] += tot;
+    __syncthreads();
+  }
+}
+
+gg_status sort_scratch_alloc(SortScratch& s, int64_t capacity) {
+  if (capacity < 1) capacity = 1;
+  s.capacity = capacity;
+  const int64_t tiles = (capacity + kSortTile - 1) / kSortTile;
+  s.hist_entries = tiles * 256;
+  // scan blocks must cover the largest scanned array: hist, cell table, particles
+  s.scan_block_entries = kScanMaxBlocks;
+  for (int i = 0; i < 2; ++i) {
+    GG_CUDA(cudaMalloc(&s.k[i], sizeof(uint32_t) * capacity));
+    GG_CUDA(cudaMalloc(&s.v[i], sizeof(uint32_t) * capacity));
+  }
+  GG_CUDA(cudaMalloc(&s.hist, sizeof(uint32_t) * s.hist_entries));
+  GG_CUDA(cudaMalloc(&s.scan_blocks, sizeof(int32_t) * s.scan_block_entries));
+  return GG_OK;
+}
+
+void sort_scratch_free(SortScratch& s) {
+  for (int i = 0; i < 2; ++i) {
+    cudaFree(s.k[i]);
+    cudaFree(s.v[i]);
+    s.k[i] = s.v[i] = nullptr;
+  }
+  cudaFree(s.hist);
+  cudaFree(s.scan_blocks);
+  s.hist = nullptr;
+  s.scan_blocks = nullptr;
+}
+
+gg_status grid_sort(const Grid& g, const float4* pos, int64_t n, SortScratch& s, uint32_t* keys_out,
+                    uint32_t* perm_out, uint32_t* keys_unsorted_out, cudaStream_t st, gg_system* prof) {
+  if (n <= 0) return GG_OK;
+  if (n > s.capacity) {
+    set_error("grid_sort: more elements than the sort scratch holds");
+    return GG_ERR_INVALID_ARGUMENT;
+  }
+  const int nn = (int)n;
+  if (prof) prof_begin(prof, PC_HASH, st);
+  k_hash<<<blocks_for(n, 256), 256, 0, st>>>(g, pos, nn, s.k[0], s.v[0], keys_unsorted_out);
+  if (s.counter) *s.counter += 1;
+  if (prof) prof_end(prof, PC_HASH, n, st);
+  if (prof) prof_begin(prof, PC_SORT, st);
+  const int bits = key_bits(g.C);
+  const int passes = (bits + 7) / 8;
+  const int tiles = (int)((n + kSortTile - 1) / kSortTile);
+  int src = 0;
+  for (int p = 0; p < passes; ++p) {
+    const int shift = 8 * p;
+    const bool last = p == passes - 1;
+    uint32_t* ko = last ? keys_out : s.k[src ^ 1];
+    uint32_t* vo = last ? perm_out : s.v[src ^ 1];
+    k_radix_hist<<<tiles, kSortThreads, 0, st>>>(s.k[src], nn, shift, tiles, s.hist);
+    gg_status rc = exclusive_scan((const int32_t*)s.hist, (int32_t*)s.hist, (int64_t)tiles * 256, s, st, nullptr);
+    if (rc != GG_OK) return rc;
+    k_radix_scatter<<<tiles, kSortThreads, 0, st>>>(s.k[src], s.v[src], ko, vo, nn, shift, tiles, s.hist);
+    if (s.counter) *s.counter += 2;
+    src ^= 1;
+  }
+  if (prof) prof_end(prof, PC_SORT, n, st);
+  GG_CUDA(cudaGetLastError());
+  return GG_OK;
+}
+
+// ------------------------------------------------------------ cell start
+
+// countingInCell_CUDA (CUDAFunctions.cuh:54-61) on the sorted keys, one
+// atomic per run of equal keys in a warp.
+__global__ void k_count_cells(const uint32_t* __restrict__ keys, int n, int32_t* __restrict__ counts) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t k = i < n ? keys[i] : 0xffffffffu;
+  const unsigned peers = __match_any_sync(0xffffffffu, k);
+  if (i < n && __popc(peers & lanemask_lt()) == 0) atomicAdd(&counts[k], __popc(peers));
+}
+
+gg_status cell_start_build(const Grid& g, const uint32_t* sorted_keys, int64_t n, int32_t* cell_start,
+                           SortScratch& s, cudaStream_t st, gg_system* prof) {
+  if (prof) prof_begin(prof, PC_CELLSTART, st);
+  GG_CUDA(cudaMemsetAsync(cell_start, 0, sizeof(int32_t) * ((int64_t)g.C + 1), st));
+  if (n > 0) {
+    k_count_cells<<<blocks_for(n, 256), 256, 0, st>>>(sorted_keys, (int)n, cell_start);
+    if (s.counter) *s.counter += 1;
+  }
+  gg_status rc = exclusive_scan(cell_start, cell_start, (int64_t)g.C + 1, s, st, nullptr);
+  if (prof) prof_end(prof, PC_CELLSTART, (int64_t)g.C + 1, st);
+  GG_CUDA(cudaGetLastError());
+  return rc;
+}
+
+// --------------------------------------------------------------- reorder
+
+// The gathers of GranularSystem.cu:97-135 for every permuted field in one
+// pass.  adaptive_last_step and merge_velocity are not permuted, as in the
+// reference.
+__global__ void k_reorder_granular(int n, const uint32_t* __restrict__ perm,
+                                   const float4* __restrict__ pos_in, float4* __restrict__ pos_out,
+                                   const float4* __restrict__ vel_in, float4* __restrict__ vel_out,
+                                   const float* __restrict__ mass_in, float* __restrict__ mass_out,
+                                   const float* __restrict__ rs_in, float* __restrict__ rs_out,
+                                   const int32_t* __restrict__ units_in, int32_t* __restrict__ units_out,
+                                   const float* __restrict__ merge_in, float* __restrict__ merge_out,
+                                   const int32_t* __restrict__ mu_in, int32_t* __restrict__ mu_out,
+                                   const int32_t* __restrict__ mc_in, int32_t* __restrict__ mc_out,
+                                   const int32_t* __restrict__ rm_in, int32_t* __restrict__ rm_out) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const uint32_t s = perm[p];
+  pos_out[p] = pos_in[s];
+  vel_out[p] = vel_in[s];
+  mass_out[p] = mass_in[s];
+  rs_out[p] = rs_in[s];
+  units_out[p] = units_in[s];
+  merge_out[p] = merge_in[s];
+  mu_out[p] = mu_in[s];
+  mc_out[p] = mc_in[s];
+  rm_out[p] = rm_in[s];
+}
+
+gg_status reorder_granular(gg_system* S, cudaStream_t st) {
+  if (S->n <= 0) return GG_OK;
+  Granular& G = S->g;
+  const int a = G.cur, b = G.cur ^ 1;
+  prof_begin(S, PC_REORDER, st);
+  k_reorder_granular<<<blocks_for(S->n, 256), 256, 0, st>>>(
+      (int)S->n, G.perm, G.pos[a], G.pos[b], G.vel[a], G.vel[b], G.mass[a], G.mass[b], G.rs[a], G.rs[b],
+      G.units[a], G.units[b], G.merge[a], G.merge[b], G.merge_units[a], G.merge_units[b],
+      G.merge_count[a], G.merge_count[b], G.remove[a], G.remove[b]);
+  count_launches(S, 1);
+  // adaptive_last_step stays where it is: copy it into the new live buffer
+  GG_CUDA(cudaMemcpyAsync(G.als[b], G.als[a], sizeof(int32_t) * S->n, cudaMemcpyDeviceToDevice, st));
+  prof_end(S, PC_REORDER, S->n, st);
+  G.cur = b;
+  GG_CUDA(cudaGetLastError());
+  return GG_OK;
+}
+
+__global__ void k_gather2(int n, const uint32_t* __restrict__ perm, const float4* __restrict__ a_in,
+                          float4* __restrict__ a_out, const float4* __restrict__ b_in,
+                          float4* __restrict__ b_out) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const uint32_t s = perm[p];
+  a_out[p] = a_in[s];
+  if (b_in) b_out[p] = b_in[s];
+}
+
+__global__ void k_gather_boundary(int n, const uint32_t* __restrict__ perm, const float4* __restrict__ p_in,
+                                  float4* __restrict__ p_out, const int32_t* __restrict__ a_in,
+                                  int32_t* __restrict__ a_out) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const uint32_t s = perm[p];
+  p_out[p] = p_in[s];
+  a_out[p] = a_in[s];
+}
+
+gg_status reorder_boundary(gg_system* S, const uint32_t* perm, cudaStream_t st) {
+  if (S->nb <= 0) return GG_OK;
+  k_gather_boundary<<<blocks_for(S->nb, 256), 256, 0, st>>>((int)S->nb, perm, S->b.pos, S->b.pos_alt,
+                                                            S->b.animated, S->b.animated_alt);
+  count_launches(S, 1);
+  std::swap(S->b.pos, S->b.pos_alt);
+  std::swap(S->b.animated, S->b.animated_alt);
+  GG_CUDA(cudaGetLastError());
+  return GG_OK;
+}
+
+gg_status reorder_upsampled(gg_system* S, const uint32_t* perm, cudaStream_t st) {
+  if (S->nu <= 0) return GG_OK;
+  const int a = S->u.cur, b = a ^ 1;
+  k_gather2<<<blocks_for(S->nu, 256), 256, 0, st>>>((int)S->nu, perm, S->u.pos[a], S->u.pos[b], S->u.vel[a],
+                                                    S->u.vel[b]);
+  count_launches(S, 1);
+  S->u.cur = b;
+  GG_CUDA(cudaGetLastError());
+  return GG_OK;
+}
+
+}  // namespace gg

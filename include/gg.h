@@ -1,0 +1,289 @@
+/*
+ * gg.h — C ABI of the GB300-native granular substep path.
+ *
+ * This header is the drop-in boundary for the per-substep simulation path of
+ * granular_gpu (src/GranularSystem.{hpp,cu}, src/Solver.{hpp,cu},
+ * src/Particles.hpp, src/GranularParticles.hpp).  The reference exposes a C++
+ * class, not a C ABI; every entry point below names the reference member it
+ * replaces.  A header-only C++ class with the reference's shape lives in
+ * granular_system.hpp and is built only on these functions.
+ *
+ * Conventions
+ *  - Every call returns a gg_status and never throws across the ABI.  The
+ *    message of the last failure on the calling thread is gg_last_error().
+ *  - A gg_system owns all of its device memory; the caller owns every host
+ *    buffer it passes.  Nothing is allocated on the device after gg_create.
+ *  - One CUDA stream per gg_system.  gg_step is asynchronous on that stream;
+ *    gg_read / gg_stats / gg_synchronize wait for it.
+ *  - One gg_system must not be used from two host threads at once.
+ *  - Positions and velocities cross the ABI as packed float[3] per particle,
+ *    the reference's float3 layout (src/Particles.hpp:19-20).
+ */
+#ifndef GG_H
+#define GG_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GG_ABI_VERSION 1
+
+typedef struct gg_system gg_system;
+typedef struct gg_grid gg_grid;
+
+typedef enum gg_status {
+  GG_OK = 0,
+  GG_ERR_INVALID_ARGUMENT = 1,
+  GG_ERR_CUDA = 2,          /* a CUDA runtime call failed */
+  GG_ERR_OUT_OF_MEMORY = 3, /* device allocation at create time failed */
+  GG_ERR_CAPACITY = 4,      /* splits would exceed max_particles; extras dropped */
+  GG_ERR_IO = 5,            /* file could not be opened / read / written */
+  GG_ERR_PARSE = 6,         /* scene JSON or snapshot is malformed */
+  GG_ERR_NUMERIC = 7,       /* a NaN/Inf position was produced (reported, not fatal) */
+  GG_ERR_NOT_SUPPORTED = 8,
+  GG_ERR_TIMEOUT = 9        /* a bounded device-side wait gave up */
+} gg_status;
+
+/* The three particle sets of src/GranularSystem.hpp:59-61. */
+typedef enum gg_set {
+  GG_SET_GRANULAR = 0,
+  GG_SET_BOUNDARY = 1,
+  GG_SET_UPSAMPLED = 2
+} gg_set;
+
+/* Per-particle fields readable with gg_read / gg_device_ptr.  Element types
+ * are given in brackets.  Fields marked (granular) exist only for that set. */
+typedef enum gg_field {
+  GG_FIELD_POS = 0,               /* float[3]  get_pos_ptr            Particles.hpp:19   */
+  GG_FIELD_VEL = 1,               /* float[3]  get_vel_ptr            Particles.hpp:20   */
+  GG_FIELD_MASS = 2,              /* float     get_mass_ptr  (granular) GranularParticles.hpp:21 */
+  GG_FIELD_MASS_UNITS = 3,        /* int32     integer mass ledger, 2^-20 of a unit mass (granular) */
+  GG_FIELD_SURFACE = 4,           /* int32     get_surface_ptr (granular) GranularParticles.hpp:23 */
+  GG_FIELD_SURFACE_DISTANCE = 5,  /* float     get_surface_distance_ptr (granular) :24 */
+  GG_FIELD_CELL_KEY = 6,          /* int32     sorted cell key of the last grid build (particle_2_cell) */
+  GG_FIELD_PERM = 7,              /* int32     pre-sort index of each sorted slot, last grid build */
+  GG_FIELD_CELL_START = 8,        /* int32[C+1] cell start table (granular or boundary) */
+  GG_FIELD_REMOVE = 9,            /* int32     Solver::_buffer_remove   (granular) */
+  GG_FIELD_MERGE = 10,            /* float     Solver::_buffer_merge    (granular) */
+  GG_FIELD_MERGE_COUNT = 11,      /* int32     Solver::_buffer_merge_count (granular) */
+  GG_FIELD_MERGE_VELOCITY = 12,   /* float[3]  Solver::_buffer_merge_velocity (granular) */
+  GG_FIELD_ADAPTIVE_LAST_STEP = 13, /* int32   get_adaptive_last_step_ptr (granular) */
+  GG_FIELD_IS_ANIMATED = 14,      /* int32     get_is_animated_ptr (boundary) */
+  GG_FIELD_CONTACTS = 15,         /* int32     contacts found by each particle in the last sweep (granular) */
+  GG_FIELD_NUM_CONSTRAINTS = 16   /* int32     constraint count n_i of the last sweep (granular) */
+} gg_field;
+
+/*
+ * Every constant the reference hard-codes on this path.  gg_default_params
+ * fills the reference's values; each field names where the value comes from.
+ */
+typedef struct gg_params {
+  int32_t stab_iters;          /* 3      pre-stabilisation sweeps, Solver.cu:428 */
+  int32_t iters;               /* 5      Jacobi sweeps, Solver.cu:99 (max_iter literal) */
+  double boundary_radius;      /* 0.01   wall particle radius (a double literal), Solver.cu:283,295,297 */
+  float boundary_min_radius;   /* 0.01   floor of the particle radius against walls, Solver.cu:281 */
+  double friction_cap;         /* 0.8    tangential cap factor (a double literal), Solver.cu:295,341 */
+  float rest_speed;            /* 0.01   speeds below are zeroed, Solver.cu:223 */
+  float damp_min_speed;        /* 1.0    Solver.cu:202 */
+  float damp_max_speed;        /* 10.0   Solver.cu:203 */
+  float damp_min;              /* 0.99   Solver.cu:204 */
+  float damp_max;              /* 0.99   Solver.cu:205 */
+  float damp_exp_rate;         /* 0.1    expf(-speed*0.1), Solver.cu:236 */
+  float adaptive_damp;         /* 0.98   extra damping after a merge/split, Solver.cu:242 */
+  float max_mass;              /* 4      GranularSystem.cu:49 */
+  float min_merge_mass;        /* 1      merge eligibility mass_i < 1, Solver.cu:542 */
+  double merge_radius;         /* 0.035  merge search radius (a double literal), Solver.cu:572,594 */
+  float surface_dist_threshold;/* 100    Solver.cu:543,578,610 */
+  float target_density;        /* 100    Solver.cu:31 */
+  int32_t blend_factor;        /* 40     Solver.hpp:11 */
+  float split_min_mass;        /* 2      split needs mass > 2, Solver.cu:795 */
+  float surface_cone;          /* 1.047197551  PI_3, GranularSystem.cu:19,598 */
+  int32_t surface_min_neighbors; /* 5    GranularSystem.cu:606 */
+  float no_surface_distance;   /* 1e5    FLT_MAX redefined, GranularSystem.cu:26 */
+  float up_inv_h2;             /* 493.8271605  r_9 = 1/0.045^2, Solver.cu:29 */
+  float up_dt;                 /* 0.002  Solver.cu:1260 */
+  float up_gravity_y;          /* -9.8   Solver.cu:1259 */
+  float up_boundary_radius;    /* 0.015  Solver.cu:1263 */
+  float up_repulsion;          /* 3.0    Solver.cu:1264 */
+  float up_max_velocity;       /* 7.0    Solver.cu:1339 */
+  float up_floor_y;            /* 0.04   Solver.cu:1354 */
+  float up_floor_friction;     /* 0.95   Solver.cu:1357 */
+  float up_boundary_damping;   /* 0.8    Solver.cu:1325 */
+  float up_ground_band;        /* 0.1    Solver.cu:1329 */
+  float up_ground_damping;     /* 0.5    Solver.cu:1330 */
+  int32_t mass_ledger;         /* 0 = float masses as the reference (Solver.cu:669-671);
+                                  1 = exact integer ledger in 2^-20 units */
+  int32_t merge_enabled;       /* 1 = merge/split active when is_adaptive */
+  int32_t upsample_enabled;    /* 1 = advect upsampled points each substep */
+  int32_t math_mode;           /* 0 = CUDA's cbrtf/expf/norm3df/rsqrtf/acosf, the functions the
+                                  reference calls; 1 = each evaluated in double and rounded once
+                                  to float (matches the CPU restatement bit for bit) */
+  int32_t reserved[7];
+} gg_params;
+
+/* Arguments of GranularSystem::GranularSystem, GranularSystem.hpp:8-14. */
+typedef struct gg_desc {
+  const float* particles;      /* n_particles x float[3] (required) */
+  int64_t n_particles;
+  const float* masses;         /* optional n_particles floats; NULL = 1.0 (GranularSystem.cu:57-58) */
+  const float* boundary;       /* n_boundary x float[3] (may be NULL if 0) */
+  int64_t n_boundary;
+  const int32_t* boundary_animated; /* optional n_boundary flags (main.cu:973-975) */
+  const float* upsampled;      /* n_upsampled x float[3] (may be NULL if 0) */
+  int64_t n_upsampled;
+  float space_size[3];
+  float cell_length;
+  float dt;
+  float gravity[3];
+  int32_t cell_size[3];
+  float density;
+  float upsampled_radius;      /* kept for readback only; unused by the step (as in the reference) */
+  int32_t is_move_boundary;
+  int32_t is_adaptive;
+  int32_t skip_initial_step;   /* 0 = the constructor runs one step (GranularSystem.cu:62) */
+  int32_t device;              /* CUDA device ordinal */
+  int64_t max_particles;       /* granular capacity; 0 = 2 x n_particles */
+  void* stream;                /* optional cudaStream_t to run on; NULL = own stream */
+  gg_params params;
+} gg_desc;
+
+/* Scene-JSON overrides for gg_create_from_scene; zero-initialise and set
+ * only the fields you want. */
+typedef struct gg_overrides {
+  int32_t has_params;          /* 1 = use params below instead of the defaults */
+  gg_params params;
+  int32_t device;
+  int64_t max_particles;
+  void* stream;
+  int32_t skip_initial_step;
+  const char* base_dir;        /* directory obj_file paths are resolved against; NULL = cwd */
+} gg_overrides;
+
+typedef struct gg_stats_t {
+  int64_t n_particles, n_boundary, n_upsampled;
+  int64_t steps;               /* completed substeps (including the constructor's) */
+  int64_t merged_last;         /* particles removed by the last adaptive step (Solver.cu:1040) */
+  int64_t split_last;          /* children appended by the last adaptive step (Solver.cu:1166) */
+  int64_t merged_total, split_total;
+  double total_mass;           /* FP64 reduction of the float masses */
+  int64_t total_mass_units;    /* integer ledger sum (mass_ledger = 1) */
+  double momentum[3];          /* FP64 sum of m v */
+  double kinetic_energy;       /* FP64 sum of m |v|^2 / 2 */
+  double center_of_mass[3];
+  float max_penetration;       /* max over particle pairs of r_i+r_j-|x_i-x_j| (>= 0) */
+  int32_t nonfinite;           /* particles with a NaN/Inf position */
+  int32_t error_word;          /* device error bits (capacity, timeout) since create */
+  int64_t launches;            /* kernels this library launched since create */
+} gg_stats_t;
+
+/* Per-kernel-class timing accumulated between gg_profile_begin/_end. */
+#define GG_PROF_MAX 24
+typedef struct gg_profile_t {
+  int32_t n_classes;
+  char names[GG_PROF_MAX][24];
+  int64_t launches[GG_PROF_MAX];
+  double ms[GG_PROF_MAX];
+  int64_t units[GG_PROF_MAX];  /* particles (or points) processed, summed over launches */
+} gg_profile_t;
+
+int32_t gg_abi_version(void);
+/* sizeof(gg_params), sizeof(gg_desc), sizeof(gg_overrides), sizeof(gg_stats_t),
+ * sizeof(gg_profile_t), in that order, for binding checks. */
+gg_status gg_struct_sizes(int64_t* sizes, int32_t n);
+const char* gg_last_error(void);
+gg_status gg_default_params(gg_params* out);
+
+/* GranularSystem::GranularSystem (GranularSystem.cu:30-63).  Unlike the
+ * reference, the caller's arrays are copied, not moved from. */
+gg_status gg_create(const gg_desc* desc, gg_system** out);
+
+/* loadSceneConfig + init_granular_system + the constructor
+ * (main.cu:123-167, 746-1173).  Reads the reference's scene-JSON keys. */
+gg_status gg_create_from_scene(const char* json_path, const gg_overrides* ov,
+                               gg_system** out);
+
+/* Builds a scene's particle sets on the host only (no GPU): the arrays
+ * init_granular_system (main.cu:746-1173) would hand to the constructor.
+ * Pass NULL buffers to query sizes.  Buffers hold float[3] per particle. */
+gg_status gg_scene_build(const char* json_path, const char* base_dir,
+                         float* particles, int64_t* n_particles,
+                         float* boundary, int32_t* boundary_animated, int64_t* n_boundary,
+                         float* upsampled, int64_t* n_upsampled,
+                         gg_desc* desc_out);
+
+/* GranularSystem::step (GranularSystem.cu:397-453), n_substeps times.
+ * Asynchronous on the system's stream. */
+gg_status gg_step(gg_system* sys, int32_t n_substeps);
+gg_status gg_synchronize(gg_system* sys);
+
+/* size() / boundary_size() / upsampled_size(), GranularSystem.hpp:21-27. */
+gg_status gg_size(gg_system* sys, gg_set set, int64_t* n);
+gg_status gg_grid_dims(gg_system* sys, int32_t cell_size[3], float* cell_length);
+
+/* Copies a field to host memory: the cudaMemcpy a caller of get_*_ptr()
+ * performs (main.cu:206-209).  capacity = elements (particles, or cells+1 for
+ * GG_FIELD_CELL_START) the buffer holds; *n receives the element count. */
+gg_status gg_read(gg_system* sys, gg_set set, gg_field field,
+                  void* host_dst, int64_t capacity, int64_t* n);
+
+/* Device pointer of a field for zero-copy use (get_*_ptr).  Valid until the
+ * next gg_step.  Positions/velocities are float[4] per particle on device
+ * (w = radius for positions); *stride_bytes receives the element stride. */
+gg_status gg_device_ptr(gg_system* sys, gg_set set, gg_field field,
+                        void** dptr, int64_t* n, int32_t* stride_bytes);
+
+/* Overwrites positions/velocities of a set from host float[3] arrays (same
+ * count as the set).  Used to start both implementations from one state. */
+gg_status gg_write(gg_system* sys, gg_set set, gg_field field,
+                   const void* host_src, int64_t n);
+
+/* Binary snapshot of the full state (all sets, solver buffers, counters). */
+gg_status gg_save(gg_system* sys, const char* path);
+gg_status gg_load(gg_system* sys, const char* path);
+
+gg_status gg_stats(gg_system* sys, gg_stats_t* out);
+
+/* Solver::save_particle_stats (Solver.cu:1444-1462): writes the per-step
+ * "Frame,MergedParticles,SplitParticles,TotalParticles" CSV. */
+gg_status gg_save_particle_stats(gg_system* sys, const char* path);
+
+/* GranularSystem::get_frame_times (GranularSystem.hpp:48): per-step device
+ * milliseconds, recorded when timing is enabled. */
+gg_status gg_set_frame_timing(gg_system* sys, int32_t enabled);
+gg_status gg_frame_times(gg_system* sys, float* host_dst, int64_t capacity, int64_t* n);
+
+/* Solver::trigger_explosion (Solver.cu:1411-1442). */
+gg_status gg_trigger_explosion(gg_system* sys, float explosion_force);
+
+/* Per-kernel-class timing with CUDA events on the system's stream. */
+gg_status gg_profile_begin(gg_system* sys);
+gg_status gg_profile_end(gg_system* sys, gg_profile_t* out);
+
+/* The system's cudaStream_t, for callers that time or order work on it. */
+gg_status gg_stream(gg_system* sys, void** stream);
+
+void gg_destroy(gg_system* sys);
+
+/*
+ * Stand-alone grid build on caller-supplied positions (device-resident
+ * scratch owned by a gg_grid).  Replaces the hash / sort_by_key / count /
+ * exclusive_scan sequence of neighbor_search_granular
+ * (GranularSystem.cu:65-173, CUDAFunctions.cuh:54-107) for parity tests of
+ * keys, sorted order and cell ranges on arbitrary inputs.
+ */
+gg_status gg_grid_create(int32_t device, int64_t capacity, const int32_t cell_size[3],
+                         float cell_length, gg_grid** out);
+/* pos: n x float[3] host.  Outputs (host, may be NULL): keys[n] (unsorted
+ * keys of the input order), sorted_keys[n], perm[n], cell_start[C+1]. */
+gg_status gg_grid_build(gg_grid* g, const float* pos, int64_t n,
+                        int32_t* keys, int32_t* sorted_keys, int32_t* perm,
+                        int32_t* cell_start);
+void gg_grid_destroy(gg_grid* g);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GG_H */

@@ -1,0 +1,175 @@
+"""ctypes wrapper of the CPU oracle (TEST INFRASTRUCTURE ONLY).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may
+import this module.  It exposes the same create/step/read surface as the
+CUDA library so parity tests read symmetrically.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from granular_gpu_gb300 import abi
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def _load(fp64: bool) -> C.CDLL:
+    name = "libggoracle64.so" if fp64 else "libggoracle32.so"
+    path = os.path.join(HERE, "_build", name)
+    if not os.path.exists(path):
+        from oracle import build as _b
+        _b.build()
+    lib = C.CDLL(path)
+    pre = "ggo64_" if fp64 else "ggo32_"
+    sig = {
+        "default_params": (None, [C.POINTER(abi.gg_params)]),
+        "create": (C.c_void_p, [C.POINTER(abi.gg_desc)]),
+        "step": (None, [C.c_void_p, C.c_int]),
+        "size": (C.c_int64, [C.c_void_p, C.c_int]),
+        "steps": (C.c_int64, [C.c_void_p]),
+        "merged_last": (C.c_int64, [C.c_void_p]),
+        "split_last": (C.c_int64, [C.c_void_p]),
+        "read": (C.c_int64, [C.c_void_p, C.c_int, C.c_int, C.c_void_p]),
+        "write": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_float), C.c_int64]),
+        "grid_build": (None, [C.POINTER(C.c_float), C.c_int64, C.POINTER(C.c_int32), C.c_float,
+                              C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                              C.POINTER(C.c_int32)]),
+        "save_particle_stats": (C.c_int, [C.c_void_p, C.c_char_p]),
+        "error_word": (C.c_int32, [C.c_void_p]),
+        "threads": (C.c_int, []),
+        "destroy": (None, [C.c_void_p]),
+    }
+    for k, (res, args) in sig.items():
+        fn = getattr(lib, pre + k)
+        fn.restype = res
+        fn.argtypes = args
+    lib._pre = pre
+    return lib
+
+
+_LIBS = {}
+
+
+def lib(fp64: bool = False) -> C.CDLL:
+    if fp64 not in _LIBS:
+        _LIBS[fp64] = _load(fp64)
+    return _LIBS[fp64]
+
+
+def _fn(l, name):
+    return getattr(l, l._pre + name)
+
+
+def _fptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_float)) if a is not None else None
+
+
+def _iptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int32)) if a is not None else None
+
+
+def grid_build(pos, cell_size, cell_length, fp64=False):
+    """keys, sorted_keys, perm, cell_start of the oracle's grid build."""
+    pos = np.ascontiguousarray(pos, dtype=np.float32).reshape(-1, 3)
+    n = pos.shape[0]
+    cs = np.ascontiguousarray(cell_size, dtype=np.int32)
+    ncell = int(cs[0]) * int(cs[1]) * int(cs[2])
+    keys = np.zeros(max(n, 1), np.int32)
+    sk = np.zeros(max(n, 1), np.int32)
+    perm = np.zeros(max(n, 1), np.int32)
+    cstart = np.zeros(ncell + 1, np.int32)
+    l = lib(fp64)
+    _fn(l, "grid_build")(_fptr(pos), n, _iptr(cs), C.c_float(cell_length),
+                         _iptr(keys), _iptr(sk), _iptr(perm), _iptr(cstart))
+    return keys[:n], sk[:n], perm[:n], cstart
+
+
+class OracleSystem:
+    """The CPU restatement behind the same surface as the CUDA system."""
+
+    def __init__(self, desc_fields: dict, fp64: bool = False):
+        self._lib = lib(fp64)
+        self._keep = []
+        d = abi.gg_desc()
+        for k, v in desc_fields.items():
+            if k in ("particles", "boundary", "upsampled", "masses"):
+                if v is None:
+                    continue
+                a = np.ascontiguousarray(v, dtype=np.float32)
+                self._keep.append(a)
+                setattr(d, k, _fptr(a))
+            elif k == "boundary_animated":
+                if v is None:
+                    continue
+                a = np.ascontiguousarray(v, dtype=np.int32)
+                self._keep.append(a)
+                d.boundary_animated = _iptr(a)
+            elif k in ("space_size", "gravity"):
+                for i in range(3):
+                    getattr(d, k)[i] = float(v[i])
+            elif k == "cell_size":
+                for i in range(3):
+                    d.cell_size[i] = int(v[i])
+            elif k == "params":
+                d.params = v
+            else:
+                setattr(d, k, v)
+        self._h = _fn(self._lib, "create")(C.byref(d))
+        self.cell_size = tuple(int(x) for x in desc_fields["cell_size"])
+
+    def step(self, n: int = 1):
+        _fn(self._lib, "step")(self._h, n)
+
+    def size(self, s: int = abi.SET_GRANULAR) -> int:
+        return int(_fn(self._lib, "size")(self._h, s))
+
+    @property
+    def steps(self):
+        return int(_fn(self._lib, "steps")(self._h))
+
+    def merged_last(self):
+        return int(_fn(self._lib, "merged_last")(self._h))
+
+    def split_last(self):
+        return int(_fn(self._lib, "split_last")(self._h))
+
+    def read(self, field: int, s: int = abi.SET_GRANULAR):
+        dt, comp = abi.FIELD_LAYOUT[field]
+        if field == abi.FIELD_CELL_START:
+            n = self.cell_size[0] * self.cell_size[1] * self.cell_size[2] + 1
+        else:
+            n = self.size(s)
+        out = np.zeros((max(n, 1), comp), dtype=dt)
+        got = _fn(self._lib, "read")(self._h, s, field, out.ctypes.data)
+        if got < 0:
+            raise KeyError(f"field {field} not available for set {s}")
+        out = out[:got]
+        return out[:, 0] if comp == 1 else out
+
+    def write(self, field: int, data, s: int = abi.SET_GRANULAR):
+        a = np.ascontiguousarray(data, dtype=np.float32).reshape(-1, 3)
+        rc = _fn(self._lib, "write")(self._h, s, field, _fptr(a), a.shape[0])
+        if rc != 0:
+            raise ValueError("oracle write failed")
+
+    def save_particle_stats(self, path: str):
+        _fn(self._lib, "save_particle_stats")(self._h, path.encode())
+
+    def error_word(self) -> int:
+        return int(_fn(self._lib, "error_word")(self._h))
+
+    def close(self):
+        if self._h:
+            _fn(self._lib, "destroy")(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def threads() -> int:
+    return int(_fn(lib(False), "threads")())

@@ -1,0 +1,83 @@
+"""The C-ABI library loads and matches include/gg.h (no GPU needed)."""
+import ctypes as C
+import os
+import re
+
+import pytest
+
+import granular_gpu_gb300 as gg
+from granular_gpu_gb300 import abi
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "gg.h")
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    names = re.findall(r"^\s*(?:const\s+)?[a-zA-Z_][a-zA-Z0-9_]*\s*\**\s+\**(gg_[a-z0-9_]+)\s*\(", text, flags=re.M)
+    return sorted(set(names))
+
+
+def test_header_declares_the_boundary():
+    names = declared_functions()
+    for required in ("gg_create", "gg_create_from_scene", "gg_step", "gg_size", "gg_read", "gg_device_ptr",
+                     "gg_save", "gg_load", "gg_stats", "gg_last_error", "gg_destroy", "gg_grid_build"):
+        assert required in names
+
+
+def test_library_exports_every_declared_symbol():
+    lib = gg.lib()
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, f"declared in gg.h but not exported: {missing}"
+    # and the Python binding declares a signature for each
+    assert not [n for n in declared_functions() if n not in abi.SIGNATURES]
+
+
+def test_struct_layouts_match_ctypes():
+    sizes = (C.c_int64 * 5)()
+    assert gg.lib().gg_struct_sizes(sizes, 5) == 0
+    assert list(sizes) == [C.sizeof(abi.gg_params), C.sizeof(abi.gg_desc), C.sizeof(abi.gg_overrides),
+                           C.sizeof(abi.gg_stats_t), C.sizeof(abi.gg_profile_t)]
+
+
+def test_default_params_match():
+    p = abi.gg_params()
+    assert gg.lib().gg_default_params(C.byref(p)) == 0
+    q = abi.default_params()
+    for name, _ in abi.gg_params._fields_:
+        a, b = getattr(p, name), getattr(q, name)
+        if name == "reserved":
+            assert list(a) == list(b)
+        elif isinstance(a, float):
+            assert C.c_float(a).value == C.c_float(b).value or a == b, name
+        else:
+            assert a == b, name
+    assert gg.lib().gg_abi_version() == 1
+
+
+def test_invalid_arguments_are_reported_without_a_gpu():
+    lib = gg.lib()
+    h = C.c_void_p()
+    assert lib.gg_create(None, C.byref(h)) == abi.GG_ERR_INVALID_ARGUMENT
+    assert b"null" in lib.gg_last_error()
+    d = abi.gg_desc()
+    d.n_particles = 1
+    assert lib.gg_create(C.byref(d), C.byref(h)) == abi.GG_ERR_INVALID_ARGUMENT
+    d.particles = (C.c_float * 3)(0.5, 0.5, 0.5)
+    d.cell_length = 0.04
+    d.cell_size[0] = d.cell_size[1] = d.cell_size[2] = 0
+    assert lib.gg_create(C.byref(d), C.byref(h)) == abi.GG_ERR_INVALID_ARGUMENT
+    assert b"cell" in lib.gg_last_error()
+    d.cell_size[0] = d.cell_size[1] = d.cell_size[2] = 2048
+    assert lib.gg_create(C.byref(d), C.byref(h)) == abi.GG_ERR_INVALID_ARGUMENT
+    d.cell_size[0] = d.cell_size[1] = d.cell_size[2] = 4
+    d.params = abi.default_params()
+    d.params.iters = 100
+    assert lib.gg_create(C.byref(d), C.byref(h)) == abi.GG_ERR_INVALID_ARGUMENT
+    assert lib.gg_step(None, 1) == abi.GG_ERR_INVALID_ARGUMENT
+
+
+def test_no_fallback_when_library_missing(tmp_path):
+    with pytest.raises(abi.NativeLibraryMissing):
+        abi.load_library(str(tmp_path / "libgg.so"))
