@@ -158,7 +158,10 @@ def run_mine(args):
         import torch.distributed as tdist
         tdist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     torch.cuda.set_device(local)
-    desc = workloads.column_collapse(seed=42 + rank)
+    counts = tuple(int(c) for c in args.counts.split(","))
+    desc = workloads.column_collapse(counts=counts, seed=42 + rank)
+    if args.math_mode:
+        desc["params"].math_mode = args.math_mode
     n0 = desc["n_particles"]
     sysg = gg.GranularSystem(**workloads.system_kwargs(desc), device=local)
     stream = torch.cuda.ExternalStream(sysg.stream, device=local)
@@ -200,6 +203,10 @@ def run_mine(args):
     value = total_units / (ms_max / 1000.0)
 
     # ---- end to end through the C ABI with pinned host buffers
+    if args.no_e2e:
+        args.steps_e2e = 0
+    else:
+        args.steps_e2e = args.steps
     n = sysg.size()
     nu = sysg.upsampled_size()
     hp = torch.empty((n, 3), dtype=torch.float32, pin_memory=True).numpy()
@@ -212,7 +219,7 @@ def run_mine(args):
     t0 = time.perf_counter()
     e2e_units = 0
     h2d = d2h = 0
-    for _ in range(args.steps):
+    for _ in range(args.steps_e2e):
         m = sysg.size()
         if hp.shape[0] != m:
             hp = torch.empty((m, 3), dtype=torch.float32, pin_memory=True).numpy()
@@ -239,7 +246,7 @@ def run_mine(args):
     if dist_on:
         tdist.all_reduce(te, op=tdist.ReduceOp.MAX)
         tdist.all_reduce(ue, op=tdist.ReduceOp.SUM)
-    e2e_value = float(ue.item()) / float(te.item())
+    e2e_value = float(ue.item()) / float(te.item()) if args.steps_e2e else None
 
     # ---- roofline of the dominant kernel class
     dom = max(prof.items(), key=lambda kv: kv[1]["ms"])
@@ -260,7 +267,8 @@ def run_mine(args):
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "particles": n0, "upsampled": desc["n_upsampled"],
+        "config": {"workload": WORKLOAD if counts == (128, 256, 256) else f"column collapse {counts}",
+                   "particles": n0, "upsampled": desc["n_upsampled"],
                    "boundary": desc["n_boundary"], "cells": int(np.prod(desc["cell_size"])),
                    "l2": "inputs larger than L2 (about 1.9 GB of particle state per step)",
                    "parallelism": f"replicas x{world}"},
@@ -293,6 +301,10 @@ def main():
     ap.add_argument("--impl", choices=["mine", "reference"], default="mine")
     ap.add_argument("--cpu-steps", type=int, default=4)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--counts", default="128,256,256",
+                    help="column lattice x,y,z (the benchmark workload is 128,256,256)")
+    ap.add_argument("--math-mode", type=int, default=0)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

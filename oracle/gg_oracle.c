@@ -925,6 +925,7 @@ int64_t GGO_SYM(size)(const ggo_sys* s, int set) {
 }
 
 int64_t GGO_SYM(steps)(const ggo_sys* s) { return s->steps; }
+int64_t GGO_SYM(n_grid)(const ggo_sys* s) { return s->n_grid; }
 int64_t GGO_SYM(merged_last)(const ggo_sys* s) { return s->merged_last; }
 int64_t GGO_SYM(split_last)(const ggo_sys* s) { return s->split_last; }
 

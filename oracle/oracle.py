@@ -28,6 +28,7 @@ def _load(fp64: bool) -> C.CDLL:
         "step": (None, [C.c_void_p, C.c_int]),
         "size": (C.c_int64, [C.c_void_p, C.c_int]),
         "steps": (C.c_int64, [C.c_void_p]),
+        "n_grid": (C.c_int64, [C.c_void_p]),
         "merged_last": (C.c_int64, [C.c_void_p]),
         "split_last": (C.c_int64, [C.c_void_p]),
         "read": (C.c_int64, [C.c_void_p, C.c_int, C.c_int, C.c_void_p]),
@@ -138,6 +139,8 @@ class OracleSystem:
         dt, comp = abi.FIELD_LAYOUT[field]
         if field == abi.FIELD_CELL_START:
             n = self.cell_size[0] * self.cell_size[1] * self.cell_size[2] + 1
+        elif field in (abi.FIELD_CELL_KEY, abi.FIELD_PERM) and s == abi.SET_GRANULAR:
+            n = max(self.size(s), int(_fn(self._lib, "n_grid")(self._h)))
         else:
             n = self.size(s)
         out = np.zeros((max(n, 1), comp), dtype=dt)

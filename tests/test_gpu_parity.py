@@ -105,10 +105,13 @@ def test_box_drop_substeps_match_oracle():
 
 
 def test_box_drop_cuda_math_within_ulps():
-    # CUDA's own transcendentals (the reference's): a few ulp from the oracle
+    # CUDA's own transcendentals (the reference's): one substep from an
+    # identical input state lands within max(1e-5 r, 4 ulp) of the oracle
     desc = workloads.box_drop(n_side=12, substeps=4, iters=3)
     s, o = _pair(desc, mode=0)
-    for k in range(1, 6):
+    for k in range(1, 8):
+        o.write(abi.FIELD_POS, s.read(gg.FIELD_POS))
+        o.write(abi.FIELD_VEL, s.read(gg.FIELD_VEL))
         s.step(1)
         o.step(1)
         _compare(s, o, k, exact=False)
