@@ -162,6 +162,7 @@ def run_mine(args):
     desc = workloads.column_collapse(counts=counts, seed=42 + rank)
     if args.math_mode:
         desc["params"].math_mode = args.math_mode
+    desc["params"].reserved[0] = args.sweep_variant
     n0 = desc["n_particles"]
     sysg = gg.GranularSystem(**workloads.system_kwargs(desc), device=local)
     stream = torch.cuda.ExternalStream(sysg.stream, device=local)
@@ -180,7 +181,6 @@ def run_mine(args):
     torch.cuda.synchronize()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     sysg.profile_begin()
-    launches0 = sysg.stats()["launches"] if "launches" in sysg.stats() else 0
     units = 0
     ev0.record(stream)
     for _ in range(args.steps):
@@ -190,9 +190,9 @@ def run_mine(args):
     torch.cuda.synchronize()
     barrier()
     prof = sysg.profile_end()
+    launches = prof.pop("_kernel_launches")
     clocks = sampler.stop()
     ms = ev0.elapsed_time(ev1)
-    launches = sysg.stats().get("launches", 0) - launches0
     t = torch.tensor([ms], dtype=torch.float64, device="cuda")
     u = torch.tensor([units], dtype=torch.float64, device="cuda")
     if dist_on:
@@ -305,6 +305,8 @@ def main():
     ap.add_argument("--counts", default="128,256,256",
                     help="column lattice x,y,z (the benchmark workload is 128,256,256)")
     ap.add_argument("--math-mode", type=int, default=0)
+    ap.add_argument("--sweep-variant", type=int, default=0,
+                    help="0 warp-cooperative, 1 one thread per particle, 2 shared-memory tile")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -265,6 +265,7 @@ class GranularSystem:
         for k in range(p.n_classes):
             name = bytes(p.names[k]).split(b"\0")[0].decode()
             out[name] = {"launches": p.launches[k], "ms": p.ms[k], "units": p.units[k]}
+        out["_kernel_launches"] = p.kernel_launches
         return out
 
     @property

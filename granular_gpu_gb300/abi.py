@@ -147,7 +147,7 @@ class gg_profile_t(C.Structure):
     _fields_ = [
         ("n_classes", C.c_int32), ("names", (C.c_char * 24) * GG_PROF_MAX),
         ("launches", C.c_int64 * GG_PROF_MAX), ("ms", C.c_double * GG_PROF_MAX),
-        ("units", C.c_int64 * GG_PROF_MAX),
+        ("units", C.c_int64 * GG_PROF_MAX), ("kernel_launches", C.c_int64),
     ]
 
 

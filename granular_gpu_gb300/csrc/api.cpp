@@ -566,6 +566,7 @@ gg_status gg_profile_begin(gg_system* S) {
   }
   S->prof_pending.clear();
   S->prof_pool_used = 0;
+  S->prof_launch_base = S->launches;
   S->profiling = true;
   return GG_OK;
 }
@@ -577,6 +578,7 @@ gg_status gg_profile_end(gg_system* S, gg_profile_t* out) {
   S->profiling = false;
   memset(out, 0, sizeof(*out));
   out->n_classes = PC_COUNT;
+  out->kernel_launches = S->launches - S->prof_launch_base;
   for (int k = 0; k < PC_COUNT && k < GG_PROF_MAX; ++k) {
     strncpy(out->names[k], prof_name(k), 23);
     out->launches[k] = S->prof_launches[k];

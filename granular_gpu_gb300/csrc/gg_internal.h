@@ -24,6 +24,7 @@ struct DevScalars {
   unsigned int rmax_bits;      // max contact radius (float bits), this step
   unsigned int inc_bits[64];   // per sweep: max |x* increment| (float bits)
   unsigned int disp0_bits;     // max |dt v| of the predict (float bits)
+  unsigned int tile_fallback;  // sweep blocks that could not use the shared-memory tile
   int error_word;              // bit0 capacity, bit1 numeric
   int n_after;                 // particle count after the adaptive step
   int n_removed;
@@ -160,6 +161,7 @@ struct gg_system {
   double prof_ms[gg::PC_COUNT] = {};
   int64_t prof_launches[gg::PC_COUNT] = {};
   int64_t prof_units[gg::PC_COUNT] = {};
+  int64_t prof_launch_base = 0;
 };
 
 struct gg_grid {

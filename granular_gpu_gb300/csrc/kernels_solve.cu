@@ -75,209 +75,6 @@ gg_status predict(gg_system* S, cudaStream_t st) {
   return GG_OK;
 }
 
-// ------------------------------------------------------------ Jacobi sweep
-
-struct SweepArgs {
-  Grid g;
-  int n;
-  int it;
-  const float4* __restrict__ xs;
-  const float* __restrict__ inv_m;
-  const uint32_t* __restrict__ keys;
-  const int32_t* __restrict__ cs;
-  const int32_t* __restrict__ bcs;
-  const float4* __restrict__ bpos;
-  float4* __restrict__ delta;
-  int32_t* __restrict__ s_extra;
-  const DevScalars* __restrict__ scal;
-  double brad;   // boundary radius (double literal 0.01)
-  double fcap;   // friction cap (double literal 0.8)
-  float minr;    // floor of the particle radius against walls (0.01f)
-};
-
-// Which of the three cell columns [c-1, c, c+1] along one axis can hold a
-// contact partner: bit k set for offset k-1.  Cells are [cL, (c+1)L) in
-// binning coordinates; a partner binned there is within R of x.
-__device__ __forceinline__ unsigned axis_mask(float x, int q, float L, float R) {
-  unsigned m = 0;
-#pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    const float lo = (float)(q + k - 1) * L;
-    const float hi = (float)(q + k) * L;
-    // NaN in x or R leaves the column in (never prunes)
-    if (!(x < lo - R) && !(x > hi + R)) m |= 1u << k;
-  }
-  return m;
-}
-
-// compute_delta_pos (Solver.cu:361-401) with boundary_constraint
-// (:272-307) and particles_constraint (:309-359), race-free.
-//
-// The reference's scatters into delta_pos[j] are overwritten by each
-// thread's final `delta_pos[i] = dp` when the grid is resident, while its
-// constraint-count increments all land.  This kernel produces exactly that
-// outcome with gathers only:
-//   delta_i = thread i's own corrections, accumulated in the reference's
-//             loop order (27 cells; walls, then particles, by index);
-//   n_i     = contacts i finds + particles that find i.
-// "j finds i" is decided here by i: i's binning cell lies in the stencil of
-// trunc(x*_j / L) (the contact test is symmetric).  When it does not, i
-// hands the count to j through s_extra (rare: only where predicted and
-// binned cells disagree).
-//
-// Cells that cannot hold a partner (farther than r_i + r_max plus the
-// largest displacement since binning) are skipped; they contribute nothing,
-// so the sum and its order are unchanged.
-template <int MM>
-__global__ void __launch_bounds__(256) k_sweep(SweepArgs a) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= a.n) return;
-  const Grid g = a.g;
-  const float4 xi4 = a.xs[i];
-  const float3 xi = f3(xi4);
-  const float rc_i = xi4.w;
-  const float rb_i = fmaxf(rc_i, a.minr);
-  const double Bd = a.brad + (double)rb_i;
-  const float Bf = (float)Bd;
-  const float inv_mi = a.inv_m[i];
-  const int3 q = trunc_cell(g, xi);
-
-  const uint32_t key_i = a.keys[i];
-  const bool binned = (int)key_i < g.C;
-  int cix = 0, ciy = 0, ciz = 0;
-  if (binned) {
-    const int nyz = g.ny * g.nz;
-    cix = (int)key_i / nyz;
-    const int r = (int)key_i - cix * nyz;
-    ciy = r / g.nz;
-    ciz = r - ciy * g.nz;
-  }
-
-  float disp = __uint_as_float(a.scal->disp0_bits);
-  for (int k = 0; k < a.it; ++k) disp += __uint_as_float(a.scal->inc_bits[k]);
-  const float rmax = __uint_as_float(a.scal->rmax_bits);
-  const float ax = fmaxf(fmaxf(fabsf(xi.x), fabsf(xi.y)), fabsf(xi.z));
-  const float slack = 4e-6f * (ax + 1.0f) + 1e-5f * g.L;
-  const float Rp = (rc_i + rmax + disp) * 1.0001f + slack;
-  const float Rb = Bf * 1.0001f + slack;
-  const unsigned pmx = axis_mask(xi.x, q.x, g.L, Rp), pmy = axis_mask(xi.y, q.y, g.L, Rp),
-                 pmz = axis_mask(xi.z, q.z, g.L, Rp);
-  const unsigned bmx = axis_mask(xi.x, q.x, g.L, Rb), bmy = axis_mask(xi.y, q.y, g.L, Rb),
-                 bmz = axis_mask(xi.z, q.z, g.L, Rb);
-  const float Bcut = Bf * Bf * 1.0001f;
-
-  float3 dp = make_float3(0.f, 0.f, 0.f);
-  int c = 0, s_loc = 0;
-  for (int ox = 0; ox < 3; ++ox) {
-    if (!(((pmx | bmx) >> ox) & 1u)) continue;
-    for (int oy = 0; oy < 3; ++oy) {
-      if (!(((pmy | bmy) >> oy) & 1u)) continue;
-      for (int oz = 0; oz < 3; ++oz) {
-        const bool usep = ((pmx >> ox) & (pmy >> oy) & (pmz >> oz) & 1u) != 0;
-        const bool useb = ((bmx >> ox) & (bmy >> oy) & (bmz >> oz) & 1u) != 0;
-        if (!usep && !useb) continue;
-        const int cell = cell_key(g, q.x + ox - 1, q.y + oy - 1, q.z + oz - 1);
-        if (cell == g.C) continue;
-        if (useb) {
-          const int b1 = a.bcs[cell + 1];
-          for (int b = a.bcs[cell]; b < b1; ++b) {
-            const float4 pb = a.bpos[b];
-            const float bx = xi.x - pb.x, by = xi.y - pb.y, bz = xi.z - pb.z;
-            const float d2 = __fmaf_rn(bx, bx, __fmaf_rn(by, by, __fmul_rn(bz, bz)));
-            if (d2 > Bcut) continue;
-            const float dis = m_norm3<MM>(bx, by, bz);
-            if (!((double)dis < Bd)) continue;  // mag < 0
-            const float mag = (float)((double)dis - Bd);
-            const float3 p12 = make_float3(bx, by, bz);
-            const float3 dpi = smul3(mag / dis, p12);
-            const float3 perp = sub3(dpi, div3s(smul3(dot3(dpi, p12), p12), dis * dis));
-            const float pn = m_norm3<MM>(perp.x, perp.y, perp.z);
-            if ((double)pn < ((double)rb_i + a.brad) * a.fcap) {
-              dp = sub3(dp, dpi);
-            } else {
-              const float minf = (float)fmin((a.brad + (double)rb_i) * a.fcap / (double)pn, 1.0);
-              dp = sub3(dp, mul3s(dpi, minf));
-            }
-            ++c;
-          }
-        }
-        if (usep) {
-          const int j1 = a.cs[cell + 1];
-          for (int j = a.cs[cell]; j < j1; ++j) {
-            if (j == i) continue;
-            const float4 xj4 = a.xs[j];
-            const float dx = xi.x - xj4.x, dy = xi.y - xj4.y, dz = xi.z - xj4.z;
-            const float rr = rc_i + xj4.w;
-            const float d2 = __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmul_rn(dz, dz)));
-            if (d2 > rr * rr * 1.0001f) continue;
-            const float dis = m_norm3<MM>(dx, dy, dz);
-            const float mag = rr - dis;
-            if (!(mag >= 0.0f)) continue;
-            const float inv_mj = a.inv_m[j];
-            // (float)(1.0 / (double)s) equals the IEEE float reciprocal of s
-            // (no double-rounding case exists for 24-bit significands).
-            const float inv_sum = __frcp_rn(inv_mi + inv_mj);
-            const float t = mag / dis;
-            const float3 p12 = make_float3(dx, dy, dz);
-            const float3 dpi = smul3((-inv_sum * inv_mi) * t, p12);
-            const float3 dpj = smul3((inv_sum * inv_mj) * t, p12);
-            const float3 dpij = sub3(dpi, dpj);
-            const float3 perp = sub3(dpij, div3s(smul3(dot3(dpij, p12), p12), dis * dis));
-            const float pn = m_norm3<MM>(perp.x, perp.y, perp.z);
-            const float w = inv_sum * inv_mi;
-            // (double)pn < (double)rr * 0.8, decided in float when clear-cut
-            const float capf = rr * (float)a.fcap;
-            bool within;
-            if (pn < capf * 0.999999f) within = true;
-            else if (pn > capf * 1.000001f) within = false;
-            else within = (double)pn < (double)rr * a.fcap;
-            if (within) {
-              dp = sub3(dp, smul3(w, dpij));
-            } else {
-              const float minf = (float)fmin((double)rr * a.fcap / (double)pn, 1.0);
-              dp = sub3(dp, mul3s(smul3(w, dpij), minf));
-            }
-            ++c;
-            const int3 qj = trunc_cell(g, make_float3(xj4.x, xj4.y, xj4.z));
-            const bool j_finds_i = binned && abs(cix - qj.x) <= 1 && abs(ciy - qj.y) <= 1 &&
-                                   abs(ciz - qj.z) <= 1;
-            if (j_finds_i) ++s_loc;
-            else atomicAdd(&a.s_extra[j], 1);
-          }
-        }
-      }
-    }
-  }
-  a.delta[i] = make_float4(dp.x, dp.y, dp.z, __int_as_float((c & 0xffff) | (s_loc << 16)));
-}
-
-gg_status sweep(gg_system* S, int it, cudaStream_t st) {
-  if (S->n <= 0) return GG_OK;
-  SweepArgs a;
-  a.g = S->grid;
-  a.n = (int)S->n;
-  a.it = it;
-  a.xs = S->g.xs;
-  a.inv_m = S->g.inv_m;
-  a.keys = S->g.keys;
-  a.cs = S->g.cell_start;
-  a.bcs = S->b.cell_start;
-  a.bpos = S->b.pos;
-  a.delta = S->g.delta;
-  a.s_extra = S->g.s_extra;
-  a.scal = S->scal;
-  a.brad = S->P.boundary_radius;
-  a.fcap = S->P.friction_cap;
-  a.minr = S->P.boundary_min_radius;
-  prof_begin(S, PC_SWEEP, st);
-  auto kern = S->P.math_mode ? k_sweep<1> : k_sweep<0>;
-  kern<<<blocks_for(S->n, 256), 256, 0, st>>>(a);
-  count_launches(S, 1);
-  prof_end(S, PC_SWEEP, S->n, st);
-  GG_CUDA(cudaGetLastError());
-  return GG_OK;
-}
-
 // change_position_functor (Solver.cu:403-414): x* += delta / max(1, n); in
 // the stabilisation sweeps x as well (:457-460).
 __global__ void k_apply(int n, float4* __restrict__ xs, float4* __restrict__ pos,

@@ -1,0 +1,542 @@
+// kernels_sweep.cu — the Jacobi contact sweep (compute_delta_pos,
+// Solver.cu:361-401, with boundary_constraint :272-307 and
+// particles_constraint :309-359), race-free, with a shared-memory tile.
+//
+// Semantics.  The reference's scatters into delta_pos[j] are overwritten by
+// each thread's final `delta_pos[i] = dp` when the whole grid is resident,
+// while its constraint-count increments all land.  This kernel produces that
+// outcome with gathers only:
+//   delta_i = thread i's own corrections, accumulated in the reference's
+//             loop order (27 cells; walls, then particles, by index);
+//   n_i     = contacts i finds + particles that find i.
+// "j finds i" is decided by i: i's binning cell lies in the stencil of
+// trunc(x*_j / L) (the contact test itself is symmetric).  When it does not,
+// i hands the count to j through s_extra (rare: only where predicted and
+// binned cells disagree).
+//
+// Pruning.  Cells that cannot hold a partner (farther than r_i + r_max plus
+// the largest displacement since binning) are skipped; they contribute
+// nothing, so the sum and its order are unchanged.
+//
+// Tiling.  Particles are sorted by cell, so a block of consecutive particles
+// covers a short z-run of one or two (x, y) columns.  The union of their
+// (pruned) stencils is a few columns x a short z-range; each is one
+// contiguous index range of the sorted arrays.  The block copies those
+// ranges (x*, radius, inverse mass) and the cell start offsets into shared
+// memory once, then every thread runs its reference loop from shared memory.
+// Blocks whose union does not fit take the same loop over global memory.
+#include <climits>
+
+#include "common.cuh"
+
+namespace gg {
+
+struct SweepArgs {
+  Grid g;
+  int n;
+  int it;
+  const float4* __restrict__ xs;
+  const float* __restrict__ inv_m;
+  const uint32_t* __restrict__ keys;
+  const int32_t* __restrict__ cs;
+  const int32_t* __restrict__ bcs;
+  const float4* __restrict__ bpos;
+  float4* __restrict__ delta;
+  int32_t* __restrict__ s_extra;
+  DevScalars* __restrict__ scal;
+  double brad;   // boundary radius (double literal 0.01)
+  double fcap;   // friction cap (double literal 0.8)
+  float minr;    // floor of the particle radius against walls (0.01f)
+};
+
+// Which of the three cell columns [c-1, c, c+1] along one axis can hold a
+// partner: bit k set for offset k-1.  Cells are [cL, (c+1)L) in binning
+// coordinates; a partner binned there is within R of x.
+__device__ __forceinline__ unsigned axis_mask(float x, int q, float L, float R) {
+  unsigned m = 0;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const float lo = (float)(q + k - 1) * L;
+    const float hi = (float)(q + k) * L;
+    // NaN in x or R leaves the column in (never prunes)
+    if (!(x < lo - R) && !(x > hi + R)) m |= 1u << k;
+  }
+  return m;
+}
+
+// Everything one target particle needs for its sweep.
+struct Target {
+  float3 x;
+  float rc, rb;
+  double Bd;      // 0.01 + r_b in double (Solver.cu:283)
+  float Bcut;     // conservative float cut for the wall test
+  float inv_m;
+  int3 q;         // query cell trunc(x*/L)
+  bool binned;
+  int cx, cy, cz; // binning cell
+  unsigned pm[3], bm[3];
+};
+
+__device__ __forceinline__ void make_target(const SweepArgs& a, int i, float4 xi4, Target& t) {
+  const Grid& g = a.g;
+  t.x = f3(xi4);
+  t.rc = xi4.w;
+  t.rb = fmaxf(t.rc, a.minr);
+  t.Bd = a.brad + (double)t.rb;
+  const float Bf = (float)t.Bd;
+  t.Bcut = Bf * Bf * 1.0001f;
+  t.inv_m = a.inv_m[i];
+  t.q = trunc_cell(g, t.x);
+  const uint32_t key = a.keys[i];
+  t.binned = (int)key < g.C;
+  t.cx = t.cy = t.cz = 0;
+  if (t.binned) {
+    const int nyz = g.ny * g.nz;
+    t.cx = (int)key / nyz;
+    const int r = (int)key - t.cx * nyz;
+    t.cy = r / g.nz;
+    t.cz = r - t.cy * g.nz;
+  }
+  float disp = __uint_as_float(a.scal->disp0_bits);
+  for (int k = 0; k < a.it; ++k) disp += __uint_as_float(a.scal->inc_bits[k]);
+  const float rmax = __uint_as_float(a.scal->rmax_bits);
+  const float ax = fmaxf(fmaxf(fabsf(t.x.x), fabsf(t.x.y)), fabsf(t.x.z));
+  const float slack = 4e-6f * (ax + 1.0f) + 1e-5f * g.L;
+  const float Rp = (t.rc + rmax + disp) * 1.0001f + slack;
+  const float Rb = Bf * 1.0001f + slack;
+  t.pm[0] = axis_mask(t.x.x, t.q.x, g.L, Rp);
+  t.pm[1] = axis_mask(t.x.y, t.q.y, g.L, Rp);
+  t.pm[2] = axis_mask(t.x.z, t.q.z, g.L, Rp);
+  t.bm[0] = axis_mask(t.x.x, t.q.x, g.L, Rb);
+  t.bm[1] = axis_mask(t.x.y, t.q.y, g.L, Rb);
+  t.bm[2] = axis_mask(t.x.z, t.q.z, g.L, Rb);
+}
+
+// boundary_constraint over one cell's wall particles (Solver.cu:272-307).
+template <int MM>
+__device__ __forceinline__ void wall_cell(const SweepArgs& a, const Target& t, int cell, float3& dp, int& c) {
+  const int b1 = a.bcs[cell + 1];
+  for (int b = a.bcs[cell]; b < b1; ++b) {
+    const float4 pb = a.bpos[b];
+    const float bx = t.x.x - pb.x, by = t.x.y - pb.y, bz = t.x.z - pb.z;
+    const float d2 = __fmaf_rn(bx, bx, __fmaf_rn(by, by, __fmul_rn(bz, bz)));
+    if (d2 > t.Bcut) continue;
+    const float dis = m_norm3<MM>(bx, by, bz);
+    if (!((double)dis < t.Bd)) continue;  // mag < 0
+    const float mag = (float)((double)dis - t.Bd);
+    const float3 p12 = make_float3(bx, by, bz);
+    const float3 dpi = smul3(mag / dis, p12);
+    const float3 perp = sub3(dpi, div3s(smul3(dot3(dpi, p12), p12), dis * dis));
+    const float pn = m_norm3<MM>(perp.x, perp.y, perp.z);
+    if ((double)pn < ((double)t.rb + a.brad) * a.fcap) {
+      dp = sub3(dp, dpi);
+    } else {
+      const float minf = (float)fmin((a.brad + (double)t.rb) * a.fcap / (double)pn, 1.0);
+      dp = sub3(dp, mul3s(dpi, minf));
+    }
+    ++c;
+  }
+}
+
+// particles_constraint for one candidate j (Solver.cu:314-357).
+template <int MM>
+__device__ __forceinline__ void particle_pair(const SweepArgs& a, const Target& t, int j, float4 xj4,
+                                              const float* inv_src, int inv_idx, float3& dp, int& c,
+                                              int& s_loc) {
+  const float dx = t.x.x - xj4.x, dy = t.x.y - xj4.y, dz = t.x.z - xj4.z;
+  const float rr = t.rc + xj4.w;
+  const float d2 = __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmul_rn(dz, dz)));
+  if (d2 > rr * rr * 1.0001f) return;
+  const float dis = m_norm3<MM>(dx, dy, dz);
+  const float mag = rr - dis;
+  if (!(mag >= 0.0f)) return;
+  const float inv_mj = inv_src[inv_idx];
+  // (float)(1.0 / (double)s) equals the IEEE float reciprocal of s (no
+  // double-rounding case exists for 24-bit significands).
+  const float inv_sum = __frcp_rn(t.inv_m + inv_mj);
+  const float tt = mag / dis;
+  const float3 p12 = make_float3(dx, dy, dz);
+  const float3 dpi = smul3((-inv_sum * t.inv_m) * tt, p12);
+  const float3 dpj = smul3((inv_sum * inv_mj) * tt, p12);
+  const float3 dpij = sub3(dpi, dpj);
+  const float3 perp = sub3(dpij, div3s(smul3(dot3(dpij, p12), p12), dis * dis));
+  const float pn = m_norm3<MM>(perp.x, perp.y, perp.z);
+  const float w = inv_sum * t.inv_m;
+  // (double)pn < (double)rr * 0.8, decided in float when clear-cut
+  const float capf = rr * (float)a.fcap;
+  bool within;
+  if (pn < capf * 0.999999f) within = true;
+  else if (pn > capf * 1.000001f) within = false;
+  else within = (double)pn < (double)rr * a.fcap;
+  if (within) {
+    dp = sub3(dp, smul3(w, dpij));
+  } else {
+    const float minf = (float)fmin((double)rr * a.fcap / (double)pn, 1.0);
+    dp = sub3(dp, mul3s(smul3(w, dpij), minf));
+  }
+  ++c;
+  const int3 qj = trunc_cell(a.g, make_float3(xj4.x, xj4.y, xj4.z));
+  const bool j_finds_i = t.binned && llabs((long long)t.cx - qj.x) <= 1 && llabs((long long)t.cy - qj.y) <= 1 &&
+                         llabs((long long)t.cz - qj.z) <= 1;
+  if (j_finds_i) ++s_loc;
+  else atomicAdd(&a.s_extra[j], 1);
+}
+
+__device__ __forceinline__ bool use_cell(const unsigned* m, int ox, int oy, int oz) {
+  return ((m[0] >> ox) & (m[1] >> oy) & (m[2] >> oz) & 1u) != 0;
+}
+
+// The reference loop for one target over global memory.
+template <int MM>
+__device__ void sweep_global(const SweepArgs& a, int i, const Target& t) {
+  const Grid& g = a.g;
+  float3 dp = make_float3(0.f, 0.f, 0.f);
+  int c = 0, s_loc = 0;
+  for (int ox = 0; ox < 3; ++ox) {
+    for (int oy = 0; oy < 3; ++oy) {
+      for (int oz = 0; oz < 3; ++oz) {
+        const bool usep = use_cell(t.pm, ox, oy, oz);
+        const bool useb = use_cell(t.bm, ox, oy, oz);
+        if (!usep && !useb) continue;
+        const int cell = cell_key(g, t.q.x + ox - 1, t.q.y + oy - 1, t.q.z + oz - 1);
+        if (cell == g.C) continue;
+        if (useb) wall_cell<MM>(a, t, cell, dp, c);
+        if (usep) {
+          const int j1 = a.cs[cell + 1];
+          for (int j = a.cs[cell]; j < j1; ++j) {
+            if (j == i) continue;
+            particle_pair<MM>(a, t, j, a.xs[j], a.inv_m, j, dp, c, s_loc);
+          }
+        }
+      }
+    }
+  }
+  a.delta[i] = make_float4(dp.x, dp.y, dp.z, __int_as_float((c & 0xffff) | (s_loc << 16)));
+}
+
+template <int MM>
+__global__ void __launch_bounds__(256) k_sweep(SweepArgs a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  Target t;
+  make_target(a, i, a.xs[i], t);
+  sweep_global<MM>(a, i, t);
+}
+
+// ------------------------------------------------------------ tiled sweep
+
+constexpr int kTileT = 128;     // particles per block
+constexpr int kTileCap = 1536;  // candidates held in shared memory
+constexpr int kTileZ = 62;      // max cells per column z-run
+constexpr int kCols = 25;       // 5 x 5 column slots around the block
+
+template <int MM>
+__global__ void __launch_bounds__(kTileT) k_sweep_tiled(SweepArgs a) {
+  __shared__ float4 s_x[kTileCap];
+  __shared__ float s_inv[kTileCap];
+  __shared__ int s_cs[kCols][kTileZ + 1];
+  __shared__ int s_zlo[kCols], s_zhi[kCols], s_idx[kCols], s_off[kCols], s_cnt[kCols];
+  __shared__ int s_bx0, s_bx1, s_by0, s_by1, s_ok;
+
+  const Grid& g = a.g;
+  const int tid = threadIdx.x;
+  const int i = blockIdx.x * kTileT + tid;
+  const bool valid = i < a.n;
+  Target t;
+  if (valid) make_target(a, i, a.xs[i], t);
+  if (tid == 0) {
+    s_bx0 = s_by0 = INT_MAX;
+    s_bx1 = s_by1 = INT_MIN;
+    s_ok = 1;
+  }
+  if (tid < kCols) {
+    s_zlo[tid] = INT_MAX;
+    s_zhi[tid] = INT_MIN;
+  }
+  __syncthreads();
+  if (valid) {
+    atomicMin(&s_bx0, t.q.x);
+    atomicMax(&s_bx1, t.q.x);
+    atomicMin(&s_by0, t.q.y);
+    atomicMax(&s_by1, t.q.y);
+  }
+  __syncthreads();
+  const int bx0 = s_bx0, by0 = s_by0;
+  // the tile covers query cells near the grid only; far-out targets (and a
+  // block spread over more than three columns per axis) take the global loop
+  const bool spread_ok = (long long)s_bx1 - bx0 <= 2 && (long long)s_by1 - by0 <= 2 && bx0 >= -1 &&
+                         s_bx1 <= g.nx && by0 >= -1 && s_by1 <= g.ny;
+  if (spread_ok && valid) {
+    // z-run of each (x, y) column this target visits after pruning
+    int zlo = INT_MAX, zhi = INT_MIN;
+    for (int oz = 0; oz < 3; ++oz)
+      if ((t.pm[2] >> oz) & 1u) {
+        zlo = min(zlo, t.q.z + oz - 1);
+        zhi = max(zhi, t.q.z + oz - 1);
+      }
+    if (zlo <= zhi)
+      for (int ox = 0; ox < 3; ++ox) {
+        if (!((t.pm[0] >> ox) & 1u)) continue;
+        for (int oy = 0; oy < 3; ++oy) {
+          if (!((t.pm[1] >> oy) & 1u)) continue;
+          const int slot = (t.q.x + ox - 1 - (bx0 - 1)) * 5 + (t.q.y + oy - 1 - (by0 - 1));
+          atomicMin(&s_zlo[slot], zlo);
+          atomicMax(&s_zhi[slot], zhi);
+        }
+      }
+  }
+  __syncthreads();
+  if (tid == 0) {
+    int ok = spread_ok ? 1 : 0;
+    int total = 0;
+    for (int s = 0; s < kCols && ok; ++s) {
+      const int cx = bx0 - 1 + s / 5, cy = by0 - 1 + s % 5;
+      int zlo = max(s_zlo[s], 0), zhi = min(s_zhi[s], g.nz - 1);
+      s_cnt[s] = 0;
+      s_off[s] = total;
+      s_idx[s] = 0;
+      if (zlo > zhi || cx < 0 || cx >= g.nx || cy < 0 || cy >= g.ny) {
+        s_zlo[s] = 1;
+        s_zhi[s] = 0;
+        continue;
+      }
+      if (zhi - zlo + 1 > kTileZ) {
+        ok = 0;
+        break;
+      }
+      const int key_lo = (cx * g.ny + cy) * g.nz + zlo;
+      const int lo = a.cs[key_lo], hi = a.cs[key_lo + (zhi - zlo + 1)];
+      s_zlo[s] = zlo;
+      s_zhi[s] = zhi;
+      s_idx[s] = lo;
+      s_cnt[s] = hi - lo;
+      total += hi - lo;
+      if (total > kTileCap) ok = 0;
+    }
+    s_ok = ok;
+  }
+  __syncthreads();
+  if (!s_ok) {
+    if (tid == 0) atomicAdd(&a.scal->tile_fallback, 1u);
+    if (valid) sweep_global<MM>(a, i, t);
+    return;
+  }
+  // stage cell starts and candidates
+  for (int s = 0; s < kCols; ++s) {
+    const int ncell = s_zhi[s] - s_zlo[s] + 1;
+    if (ncell <= 0) continue;
+    const int cx = bx0 - 1 + s / 5, cy = by0 - 1 + s % 5;
+    const int key_lo = (cx * g.ny + cy) * g.nz + s_zlo[s];
+    for (int k = tid; k <= ncell; k += kTileT) s_cs[s][k] = a.cs[key_lo + k];
+    const int base = s_idx[s], off = s_off[s], cnt = s_cnt[s];
+    for (int k = tid; k < cnt; k += kTileT) {
+      s_x[off + k] = a.xs[base + k];
+      s_inv[off + k] = a.inv_m[base + k];
+    }
+  }
+  __syncthreads();
+  if (!valid) return;
+
+  float3 dp = make_float3(0.f, 0.f, 0.f);
+  int c = 0, s_loc = 0;
+  for (int ox = 0; ox < 3; ++ox) {
+    for (int oy = 0; oy < 3; ++oy) {
+      for (int oz = 0; oz < 3; ++oz) {
+        const bool usep = use_cell(t.pm, ox, oy, oz);
+        const bool useb = use_cell(t.bm, ox, oy, oz);
+        if (!usep && !useb) continue;
+        const int cx = t.q.x + ox - 1, cy = t.q.y + oy - 1, cz = t.q.z + oz - 1;
+        const int cell = cell_key(g, cx, cy, cz);
+        if (cell == g.C) continue;
+        if (useb) wall_cell<MM>(a, t, cell, dp, c);
+        if (usep) {
+          const int s = (cx - (bx0 - 1)) * 5 + (cy - (by0 - 1));
+          const int zr = cz - s_zlo[s];
+          const int j0 = s_cs[s][zr], j1 = s_cs[s][zr + 1];
+          const int shift = s_off[s] - s_idx[s];
+          for (int j = j0; j < j1; ++j) {
+            if (j == i) continue;
+            particle_pair<MM>(a, t, j, s_x[j + shift], s_inv, j + shift, dp, c, s_loc);
+          }
+        }
+      }
+    }
+  }
+  a.delta[i] = make_float4(dp.x, dp.y, dp.z, __int_as_float((c & 0xffff) | (s_loc << 16)));
+}
+
+// ------------------------------------------------------------ warp sweep
+//
+// The reference sums a particle's corrections over its 27 cells in the
+// order m = (dx+1)*9 + (dy+1)*3 + (dz+1) and, inside a cell, walls then
+// particles by index.  Because the cell key is lexicographic in (x, y, z),
+// that order is increasing cell key, and particles are stored by key: a
+// lane's reference order is increasing key, walls before particles of the
+// same cell.  A warp therefore visits the union of its lanes' stencils in
+// key order, every candidate loaded once for the whole warp; each lane keeps
+// the candidates that pass a cheap distance test in a list (in order), and
+// the lanes then process their k-th listed candidate together.
+
+constexpr int kWarpList = 32;      // listed candidates per lane before a flush
+constexpr int kWarpThreads = 256;
+
+template <int MM>
+__device__ __forceinline__ void process_entry(const SweepArgs& a, const Target& t, int i, int e, float3& dp,
+                                              int& c, int& s_loc) {
+  if (e < 0) {
+    // one wall particle (the exact test of boundary_constraint)
+    const int b = -e - 1;
+    const float4 pb = a.bpos[b];
+    const float bx = t.x.x - pb.x, by = t.x.y - pb.y, bz = t.x.z - pb.z;
+    const float dis = m_norm3<MM>(bx, by, bz);
+    if (!((double)dis < t.Bd)) return;
+    const float mag = (float)((double)dis - t.Bd);
+    const float3 p12 = make_float3(bx, by, bz);
+    const float3 dpi = smul3(mag / dis, p12);
+    const float3 perp = sub3(dpi, div3s(smul3(dot3(dpi, p12), p12), dis * dis));
+    const float pn = m_norm3<MM>(perp.x, perp.y, perp.z);
+    if ((double)pn < ((double)t.rb + a.brad) * a.fcap) {
+      dp = sub3(dp, dpi);
+    } else {
+      const float minf = (float)fmin((a.brad + (double)t.rb) * a.fcap / (double)pn, 1.0);
+      dp = sub3(dp, mul3s(dpi, minf));
+    }
+    ++c;
+  } else {
+    particle_pair<MM>(a, t, e, a.xs[e], a.inv_m, e, dp, c, s_loc);
+  }
+}
+
+template <int MM>
+__global__ void __launch_bounds__(kWarpThreads) k_sweep_warp(SweepArgs a) {
+  __shared__ int s_list[kWarpThreads / 32][kWarpList][32];
+  const Grid& g = a.g;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int i = blockIdx.x * kWarpThreads + threadIdx.x;
+  const bool valid = i < a.n;
+  Target t;
+  if (valid) make_target(a, i, a.xs[i], t);
+  float3 dp = make_float3(0.f, 0.f, 0.f);
+  int c = 0, s_loc = 0, cnt = 0;
+  // lane's visited z offsets (particles or walls)
+  const unsigned mz = valid ? (t.pm[2] | t.bm[2]) : 0u;
+  const unsigned mxy0 = valid ? (t.pm[0] | t.bm[0]) : 0u, mxy1 = valid ? (t.pm[1] | t.bm[1]) : 0u;
+  int zoff_lo = 2, zoff_hi = -2;
+  for (int k = 0; k < 3; ++k)
+    if ((mz >> k) & 1u) {
+      zoff_lo = min(zoff_lo, k - 1);
+      zoff_hi = max(zoff_hi, k - 1);
+    }
+
+  auto flush = [&]() {
+    for (int k = 0; k < cnt; ++k) process_entry<MM>(a, t, i, s_list[w][k][lane], dp, c, s_loc);
+    cnt = 0;
+  };
+  auto push = [&](int e) {
+    if (cnt == kWarpList) flush();
+    s_list[w][cnt++][lane] = e;
+  };
+
+  unsigned pending = __ballot_sync(0xffffffffu, valid);
+  while (pending) {
+    const int leader = __ffs(pending) - 1;
+    const int gx = __shfl_sync(0xffffffffu, t.q.x, leader);
+    const int gy = __shfl_sync(0xffffffffu, t.q.y, leader);
+    const bool mine = valid && ((pending >> lane) & 1u) && t.q.x == gx && t.q.y == gy;
+    const unsigned members = __ballot_sync(0xffffffffu, mine);
+    pending &= ~members;
+    for (int ox = 0; ox < 3; ++ox) {
+      for (int oy = 0; oy < 3; ++oy) {
+        const bool colin = mine && ((mxy0 >> ox) & 1u) && ((mxy1 >> oy) & 1u);
+        if (!__any_sync(0xffffffffu, colin)) continue;
+        const long long cxl = (long long)gx + ox - 1, cyl = (long long)gy + oy - 1;
+        if (cxl < 0 || cxl >= g.nx || cyl < 0 || cyl >= g.ny) continue;
+        const int cx = (int)cxl, cy = (int)cyl;
+        int zl = colin ? t.q.z + zoff_lo : INT_MAX;
+        int zh = colin ? t.q.z + zoff_hi : INT_MIN;
+        for (int o = 16; o > 0; o >>= 1) {
+          zl = min(zl, __shfl_xor_sync(0xffffffffu, zl, o));
+          zh = max(zh, __shfl_xor_sync(0xffffffffu, zh, o));
+        }
+        zl = max(zl, 0);
+        zh = min(zh, g.nz - 1);
+        for (int cz = zl; cz <= zh; ++cz) {
+          const int oz = cz - t.q.z + 1;
+          const bool zin = colin && oz >= 0 && oz <= 2;
+          const bool usep = zin && use_cell(t.pm, ox, oy, oz);
+          const bool useb = zin && use_cell(t.bm, ox, oy, oz);
+          const unsigned anyb = __ballot_sync(0xffffffffu, useb);
+          const unsigned anyp = __ballot_sync(0xffffffffu, usep);
+          if (!(anyb | anyp)) continue;
+          const int cell = (cx * g.ny + cy) * g.nz + cz;
+          if (anyb) {
+            const int b1 = a.bcs[cell + 1];
+            for (int b = a.bcs[cell]; b < b1; ++b) {
+              const float4 pb = a.bpos[b];
+              if (useb) {
+                const float bx = t.x.x - pb.x, by = t.x.y - pb.y, bz = t.x.z - pb.z;
+                const float d2 = __fmaf_rn(bx, bx, __fmaf_rn(by, by, __fmul_rn(bz, bz)));
+                if (!(d2 > t.Bcut)) push(-b - 1);
+              }
+            }
+          }
+          if (anyp) {
+            const int j1 = a.cs[cell + 1];
+            for (int j = a.cs[cell]; j < j1; ++j) {
+              const float4 xj = a.xs[j];
+              if (usep && j != i) {
+                const float dx = t.x.x - xj.x, dy = t.x.y - xj.y, dz = t.x.z - xj.z;
+                const float rr = t.rc + xj.w;
+                const float d2 = __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmul_rn(dz, dz)));
+                if (!(d2 > rr * rr * 1.0001f)) push(j);
+              }
+            }
+          }
+        }
+      }
+    }
+  }
+  if (valid) {
+    flush();
+    a.delta[i] = make_float4(dp.x, dp.y, dp.z, __int_as_float((c & 0xffff) | (s_loc << 16)));
+  }
+}
+
+gg_status sweep(gg_system* S, int it, cudaStream_t st) {
+  if (S->n <= 0) return GG_OK;
+  SweepArgs a;
+  a.g = S->grid;
+  a.n = (int)S->n;
+  a.it = it;
+  a.xs = S->g.xs;
+  a.inv_m = S->g.inv_m;
+  a.keys = S->g.keys;
+  a.cs = S->g.cell_start;
+  a.bcs = S->b.cell_start;
+  a.bpos = S->b.pos;
+  a.delta = S->g.delta;
+  a.s_extra = S->g.s_extra;
+  a.scal = S->scal;
+  a.brad = S->P.boundary_radius;
+  a.fcap = S->P.friction_cap;
+  a.minr = S->P.boundary_min_radius;
+  prof_begin(S, PC_SWEEP, st);
+  // reserved[0] selects a variant for comparison: 0 warp-cooperative
+  // (default), 1 one thread per particle over global memory, 2 shared tile
+  if (S->P.reserved[0] == 1) {
+    auto kern = S->P.math_mode ? k_sweep<1> : k_sweep<0>;
+    kern<<<blocks_for(S->n, 256), 256, 0, st>>>(a);
+  } else if (S->P.reserved[0] == 2) {
+    auto kern = S->P.math_mode ? k_sweep_tiled<1> : k_sweep_tiled<0>;
+    kern<<<blocks_for(S->n, kTileT), kTileT, 0, st>>>(a);
+  } else {
+    auto kern = S->P.math_mode ? k_sweep_warp<1> : k_sweep_warp<0>;
+    kern<<<blocks_for(S->n, kWarpThreads), kWarpThreads, 0, st>>>(a);
+  }
+  count_launches(S, 1);
+  prof_end(S, PC_SWEEP, S->n, st);
+  GG_CUDA(cudaGetLastError());
+  return GG_OK;
+}
+
+}  // namespace gg

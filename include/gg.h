@@ -186,6 +186,7 @@ typedef struct gg_profile_t {
   int64_t launches[GG_PROF_MAX];
   double ms[GG_PROF_MAX];
   int64_t units[GG_PROF_MAX];  /* particles (or points) processed, summed over launches */
+  int64_t kernel_launches;     /* kernels launched between begin and end */
 } gg_profile_t;
 
 int32_t gg_abi_version(void);

@@ -33,4 +33,4 @@ def test_shim_runs_reference_style_caller(tmp_path):
     assert "n=1000" in lines[0] and "up=25000" in lines[0]
     ys = [float(l.split("com_y=")[1]) for l in lines]
     assert ys[-1] < ys[0], "the block falls"
-    assert "frames=5" in r.stdout  # the constructor's step plus four
+    assert "frames=4" in r.stdout  # frame timing starts after the constructor's step

@@ -104,6 +104,29 @@ def test_box_drop_substeps_match_oracle():
     assert s.read(gg.FIELD_CONTACTS).sum() > 0, "the test scene must produce contacts"
 
 
+@pytest.mark.parametrize("variant", [0, 1, 2])
+def test_sweep_variants_bit_exact(variant):
+    # warp-cooperative (0), one thread per particle (1), shared tile (2)
+    desc = workloads.box_drop(n_side=16, substeps=4, iters=5, adaptive=1, upsample_per=2)
+    desc["params"].reserved[0] = variant
+    s, o = _pair(desc)
+    for k in range(1, 8):
+        s.step(1)
+        o.step(1)
+        _compare(s, o, k)
+
+
+def test_sweep_column_scene_bit_exact():
+    # the benchmark scene's geometry (walls, 2x1x1 box, r = 0.002) at a size
+    # the oracle finishes quickly
+    desc = workloads.column_collapse(counts=(24, 40, 32), upsample_per=2)
+    s, o = _pair(desc)
+    for k in range(1, 5):
+        s.step(1)
+        o.step(1)
+        _compare(s, o, k)
+
+
 def test_box_drop_cuda_math_within_ulps():
     # CUDA's own transcendentals (the reference's): one substep from an
     # identical input state lands within max(1e-5 r, 4 ulp) of the oracle
