@@ -163,6 +163,7 @@ def run_mine(args):
     if args.math_mode:
         desc["params"].math_mode = args.math_mode
     desc["params"].reserved[0] = args.sweep_variant
+    desc["params"].reserved[1] = args.stencil_variant
     n0 = desc["n_particles"]
     sysg = gg.GranularSystem(**workloads.system_kwargs(desc), device=local)
     stream = torch.cuda.ExternalStream(sysg.stream, device=local)
@@ -307,6 +308,8 @@ def main():
     ap.add_argument("--math-mode", type=int, default=0)
     ap.add_argument("--sweep-variant", type=int, default=0,
                     help="0 warp-cooperative, 1 one thread per particle, 2 shared-memory tile")
+    ap.add_argument("--stencil-variant", type=int, default=0,
+                    help="surface/distance/merge/upsampling: 0 warp-cooperative, 1 one thread per particle")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -159,15 +159,25 @@ __device__ __forceinline__ void particle_pair(const SweepArgs& a, const Target& 
   const float3 dpi = smul3((-inv_sum * t.inv_m) * tt, p12);
   const float3 dpj = smul3((inv_sum * inv_mj) * tt, p12);
   const float3 dpij = sub3(dpi, dpj);
-  const float3 perp = sub3(dpij, div3s(smul3(dot3(dpij, p12), p12), dis * dis));
-  const float pn = m_norm3<MM>(perp.x, perp.y, perp.z);
   const float w = inv_sum * t.inv_m;
-  // (double)pn < (double)rr * 0.8, decided in float when clear-cut
   const float capf = rr * (float)a.fcap;
+  // The tangential part `perp` of dpij (which is parallel to p12) is
+  // rounding noise: |perp| <= 2 (|a| + |b|) dis (1 + 8 eps) with a, b the
+  // two scalar factors above.  When that bound is below the cap the
+  // reference's branch is decided and perp need not be formed.
+  const float bound = 2.0001f * (fabsf((-inv_sum * t.inv_m) * tt) + fabsf((inv_sum * inv_mj) * tt)) * dis;
   bool within;
-  if (pn < capf * 0.999999f) within = true;
-  else if (pn > capf * 1.000001f) within = false;
-  else within = (double)pn < (double)rr * a.fcap;
+  float pn = 0.0f;
+  if (bound < capf * 0.999f) {
+    within = true;
+  } else {
+    const float3 perp = sub3(dpij, div3s(smul3(dot3(dpij, p12), p12), dis * dis));
+    pn = m_norm3<MM>(perp.x, perp.y, perp.z);
+    // (double)pn < (double)rr * 0.8, decided in float when clear-cut
+    if (pn < capf * 0.999999f) within = true;
+    else if (pn > capf * 1.000001f) within = false;
+    else within = (double)pn < (double)rr * a.fcap;
+  }
   if (within) {
     dp = sub3(dp, smul3(w, dpij));
   } else {
@@ -408,8 +418,9 @@ __device__ __forceinline__ void process_entry(const SweepArgs& a, const Target& 
 }
 
 template <int MM>
-__global__ void __launch_bounds__(kWarpThreads) k_sweep_warp(SweepArgs a) {
+__global__ void __launch_bounds__(kWarpThreads, 2) k_sweep_warp(SweepArgs a) {
   __shared__ int s_list[kWarpThreads / 32][kWarpList][32];
+  __shared__ float4 s_cand[kWarpThreads / 32][32];
   const Grid& g = a.g;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int i = blockIdx.x * kWarpThreads + threadIdx.x;
@@ -460,38 +471,62 @@ __global__ void __launch_bounds__(kWarpThreads) k_sweep_warp(SweepArgs a) {
         }
         zl = max(zl, 0);
         zh = min(zh, g.nz - 1);
-        for (int cz = zl; cz <= zh; ++cz) {
+        if (zl > zh) continue;
+        const int key0 = (cx * g.ny + cy) * g.nz + zl;
+        // per-cell membership of this lane
+        auto in_p = [&](int cz) {
           const int oz = cz - t.q.z + 1;
-          const bool zin = colin && oz >= 0 && oz <= 2;
-          const bool usep = zin && use_cell(t.pm, ox, oy, oz);
-          const bool useb = zin && use_cell(t.bm, ox, oy, oz);
-          const unsigned anyb = __ballot_sync(0xffffffffu, useb);
-          const unsigned anyp = __ballot_sync(0xffffffffu, usep);
-          if (!(anyb | anyp)) continue;
-          const int cell = (cx * g.ny + cy) * g.nz + cz;
-          if (anyb) {
-            const int b1 = a.bcs[cell + 1];
-            for (int b = a.bcs[cell]; b < b1; ++b) {
-              const float4 pb = a.bpos[b];
-              if (useb) {
-                const float bx = t.x.x - pb.x, by = t.x.y - pb.y, bz = t.x.z - pb.z;
-                const float d2 = __fmaf_rn(bx, bx, __fmaf_rn(by, by, __fmul_rn(bz, bz)));
-                if (!(d2 > t.Bcut)) push(-b - 1);
-              }
+          return colin && oz >= 0 && oz <= 2 && use_cell(t.pm, ox, oy, oz);
+        };
+        auto walls = [&](int cz) {
+          const int oz = cz - t.q.z + 1;
+          const bool useb = colin && oz >= 0 && oz <= 2 && use_cell(t.bm, ox, oy, oz);
+          if (!__any_sync(0xffffffffu, useb)) return;
+          const int cell = key0 + (cz - zl);
+          const int b1 = a.bcs[cell + 1];
+          for (int b = a.bcs[cell]; b < b1; ++b) {
+            const float4 pb = a.bpos[b];
+            if (useb) {
+              const float bx = t.x.x - pb.x, by = t.x.y - pb.y, bz = t.x.z - pb.z;
+              const float d2 = __fmaf_rn(bx, bx, __fmaf_rn(by, by, __fmul_rn(bz, bz)));
+              if (!(d2 > t.Bcut)) push(-b - 1);
             }
           }
-          if (anyp) {
-            const int j1 = a.cs[cell + 1];
-            for (int j = a.cs[cell]; j < j1; ++j) {
-              const float4 xj = a.xs[j];
-              if (usep && j != i) {
-                const float dx = t.x.x - xj.x, dy = t.x.y - xj.y, dz = t.x.z - xj.z;
-                const float rr = t.rc + xj.w;
-                const float d2 = __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmul_rn(dz, dz)));
-                if (!(d2 > rr * rr * 1.0001f)) push(j);
-              }
+        };
+        // the z-run is one contiguous index range of the sorted particles;
+        // cells are entered in order and their walls come first
+        const int J1 = a.cs[key0 + (zh - zl + 1)];
+        int cz = zl;
+        int cnext = a.cs[key0 + 1];
+        walls(cz);
+        bool inp = in_p(cz);
+        for (int base = a.cs[key0]; base < J1; base += 32) {
+          const int jl = base + lane;
+          if (jl < J1) s_cand[w][lane] = a.xs[jl];
+          __syncwarp();
+          const int m = min(32, J1 - base);
+          for (int k = 0; k < m; ++k) {
+            const int j = base + k;
+            while (j >= cnext) {
+              ++cz;
+              cnext = a.cs[key0 + (cz - zl) + 1];
+              walls(cz);
+              inp = in_p(cz);
+            }
+            if (inp && j != i) {
+              const float4 xj = s_cand[w][k];
+              const float dx = t.x.x - xj.x, dy = t.x.y - xj.y, dz = t.x.z - xj.z;
+              const float rr = t.rc + xj.w;
+              const float d2 = __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmul_rn(dz, dz)));
+              if (!(d2 > rr * rr * 1.0001f)) push(j);
             }
           }
+          __syncwarp();
+        }
+        // cells after the last particle of the run may still hold walls
+        while (cz < zh) {
+          ++cz;
+          walls(cz);
         }
       }
     }
