@@ -112,7 +112,7 @@ gg_status surface(gg_system* S, cudaStream_t st) {
   if (S->n <= 0) return GG_OK;
   const int c = S->g.cur;
   prof_begin(S, PC_SURFACE, st);
-  auto kern = S->P.reserved[1] == 1 ? (S->P.math_mode ? k_surface<1> : k_surface<0>)
+  auto kern = S->P.reserved[1] != 1 ? (S->P.math_mode ? k_surface<1> : k_surface<0>)
                                     : (S->P.math_mode ? k_surface_warp<1> : k_surface_warp<0>);
   kern<<<blocks_for(S->n, 256), 256, 0, st>>>(S->grid, (int)S->n, S->g.pos[c], S->g.rs[c], S->g.cell_start,
                                                    S->g.surface, S->P.surface_cone, S->P.surface_min_neighbors);
@@ -187,7 +187,7 @@ __global__ void __launch_bounds__(256) k_surfdist_warp(Grid g, int n, const floa
 gg_status surface_distance(gg_system* S, cudaStream_t st) {
   if (S->n <= 0) return GG_OK;
   prof_begin(S, PC_SURFDIST, st);
-  auto kern = S->P.reserved[1] == 1 ? k_surfdist : k_surfdist_warp;
+  auto kern = S->P.reserved[1] != 1 ? k_surfdist : k_surfdist_warp;
   kern<<<blocks_for(S->n, 256), 256, 0, st>>>(S->grid, (int)S->n, S->g.pos[S->g.cur], S->g.surface,
                                                     S->g.cell_start, S->g.sdist, S->P.no_surface_distance);
   count_launches(S, 1);
@@ -397,7 +397,7 @@ gg_status merge_mark(gg_system* S, cudaStream_t st) {
   }
   const int nb = blocks_for(S->n, 256);
   prof_begin(S, PC_MERGE, st);
-  if (S->P.reserved[1] == 1) k_merge_scan<<<nb, 256, 0, st>>>(a);
+  if (S->P.reserved[1] != 1) k_merge_scan<<<nb, 256, 0, st>>>(a);
   else k_merge_scan_warp<<<nb, 256, 0, st>>>(a);
   k_merge_winner<<<nb, 256, 0, st>>>(a);
   k_merge_apply<<<nb, 256, 0, st>>>(a);

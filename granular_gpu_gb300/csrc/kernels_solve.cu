@@ -398,7 +398,7 @@ gg_status upsample(gg_system* S, cudaStream_t st) {
   a.band = S->P.up_ground_band;
   a.gdamp = S->P.up_ground_damping;
   prof_begin(S, PC_UPSAMPLE, st);
-  if (S->P.reserved[1] == 1) k_upsample<<<blocks_for(S->nu, 256), 256, 0, st>>>(a);
+  if (S->P.reserved[1] != 1) k_upsample<<<blocks_for(S->nu, 256), 256, 0, st>>>(a);
   else k_upsample_warp<<<blocks_for(S->nu, 256), 256, 0, st>>>(a);
   count_launches(S, 1);
   prof_end(S, PC_UPSAMPLE, S->nu, st);

@@ -418,7 +418,7 @@ __device__ __forceinline__ void process_entry(const SweepArgs& a, const Target& 
 }
 
 template <int MM>
-__global__ void __launch_bounds__(kWarpThreads, 2) k_sweep_warp(SweepArgs a) {
+__global__ void __launch_bounds__(kWarpThreads, 2) k_sweep_warp_staged(SweepArgs a) {
   __shared__ int s_list[kWarpThreads / 32][kWarpList][32];
   __shared__ float4 s_cand[kWarpThreads / 32][32];
   const Grid& g = a.g;
@@ -537,6 +537,150 @@ __global__ void __launch_bounds__(kWarpThreads, 2) k_sweep_warp(SweepArgs a) {
   }
 }
 
+template <int MM>
+__global__ void __launch_bounds__(kWarpThreads) k_sweep_warp_direct(SweepArgs a) {
+  __shared__ int s_list[kWarpThreads / 32][kWarpList][32];
+  const Grid& g = a.g;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int i = blockIdx.x * kWarpThreads + threadIdx.x;
+  const bool valid = i < a.n;
+  Target t;
+  if (valid) make_target(a, i, a.xs[i], t);
+  float3 dp = make_float3(0.f, 0.f, 0.f);
+  int c = 0, s_loc = 0, cnt = 0;
+  // lane's visited z offsets (particles or walls)
+  const unsigned mz = valid ? (t.pm[2] | t.bm[2]) : 0u;
+  const unsigned mxy0 = valid ? (t.pm[0] | t.bm[0]) : 0u, mxy1 = valid ? (t.pm[1] | t.bm[1]) : 0u;
+  int zoff_lo = 2, zoff_hi = -2;
+  for (int k = 0; k < 3; ++k)
+    if ((mz >> k) & 1u) {
+      zoff_lo = min(zoff_lo, k - 1);
+      zoff_hi = max(zoff_hi, k - 1);
+    }
+
+  auto flush = [&]() {
+    for (int k = 0; k < cnt; ++k) process_entry<MM>(a, t, i, s_list[w][k][lane], dp, c, s_loc);
+    cnt = 0;
+  };
+  auto push = [&](int e) {
+    if (cnt == kWarpList) flush();
+    s_list[w][cnt++][lane] = e;
+  };
+
+  unsigned pending = __ballot_sync(0xffffffffu, valid);
+  while (pending) {
+    const int leader = __ffs(pending) - 1;
+    const int gx = __shfl_sync(0xffffffffu, t.q.x, leader);
+    const int gy = __shfl_sync(0xffffffffu, t.q.y, leader);
+    const bool mine = valid && ((pending >> lane) & 1u) && t.q.x == gx && t.q.y == gy;
+    const unsigned members = __ballot_sync(0xffffffffu, mine);
+    pending &= ~members;
+    for (int ox = 0; ox < 3; ++ox) {
+      for (int oy = 0; oy < 3; ++oy) {
+        const bool colin = mine && ((mxy0 >> ox) & 1u) && ((mxy1 >> oy) & 1u);
+        if (!__any_sync(0xffffffffu, colin)) continue;
+        const long long cxl = (long long)gx + ox - 1, cyl = (long long)gy + oy - 1;
+        if (cxl < 0 || cxl >= g.nx || cyl < 0 || cyl >= g.ny) continue;
+        const int cx = (int)cxl, cy = (int)cyl;
+        int zl = colin ? t.q.z + zoff_lo : INT_MAX;
+        int zh = colin ? t.q.z + zoff_hi : INT_MIN;
+        for (int o = 16; o > 0; o >>= 1) {
+          zl = min(zl, __shfl_xor_sync(0xffffffffu, zl, o));
+          zh = max(zh, __shfl_xor_sync(0xffffffffu, zh, o));
+        }
+        zl = max(zl, 0);
+        zh = min(zh, g.nz - 1);
+        for (int cz = zl; cz <= zh; ++cz) {
+          const int oz = cz - t.q.z + 1;
+          const bool zin = colin && oz >= 0 && oz <= 2;
+          const bool usep = zin && use_cell(t.pm, ox, oy, oz);
+          const bool useb = zin && use_cell(t.bm, ox, oy, oz);
+          const unsigned anyb = __ballot_sync(0xffffffffu, useb);
+          const unsigned anyp = __ballot_sync(0xffffffffu, usep);
+          if (!(anyb | anyp)) continue;
+          const int cell = (cx * g.ny + cy) * g.nz + cz;
+          if (anyb) {
+            const int b1 = a.bcs[cell + 1];
+            for (int b = a.bcs[cell]; b < b1; ++b) {
+              const float4 pb = a.bpos[b];
+              if (useb) {
+                const float bx = t.x.x - pb.x, by = t.x.y - pb.y, bz = t.x.z - pb.z;
+                const float d2 = __fmaf_rn(bx, bx, __fmaf_rn(by, by, __fmul_rn(bz, bz)));
+                if (!(d2 > t.Bcut)) push(-b - 1);
+              }
+            }
+          }
+          if (anyp) {
+            const int j1 = a.cs[cell + 1];
+            for (int j = a.cs[cell]; j < j1; ++j) {
+              const float4 xj = a.xs[j];
+              if (usep && j != i) {
+                const float dx = t.x.x - xj.x, dy = t.x.y - xj.y, dz = t.x.z - xj.z;
+                const float rr = t.rc + xj.w;
+                const float d2 = __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmul_rn(dz, dz)));
+                if (!(d2 > rr * rr * 1.0001f)) push(j);
+              }
+            }
+          }
+        }
+      }
+    }
+  }
+  if (valid) {
+    flush();
+    a.delta[i] = make_float4(dp.x, dp.y, dp.z, __int_as_float((c & 0xffff) | (s_loc << 16)));
+  }
+}
+
+// One thread per particle over all 27 cells (no per-lane pruning, so the
+// lanes of a warp walk the same cell sequence), with the candidates that
+// pass the cheap distance test listed in order and processed by all lanes
+// together afterwards.
+template <int MM>
+__global__ void __launch_bounds__(kWarpThreads) k_sweep_list(SweepArgs a) {
+  __shared__ int s_list[kWarpThreads / 32][kWarpList][32];
+  const Grid& g = a.g;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int i = blockIdx.x * kWarpThreads + threadIdx.x;
+  if (i >= a.n) return;
+  Target t;
+  make_target(a, i, a.xs[i], t);
+  float3 dp = make_float3(0.f, 0.f, 0.f);
+  int c = 0, s_loc = 0, cnt = 0;
+  auto flush = [&]() {
+    for (int k = 0; k < cnt; ++k) process_entry<MM>(a, t, i, s_list[w][k][lane], dp, c, s_loc);
+    cnt = 0;
+  };
+  auto push = [&](int e) {
+    if (cnt == kWarpList) flush();
+    s_list[w][cnt++][lane] = e;
+  };
+  for (int m = 0; m < 27; ++m) {
+    const int ox = m / 9, oy = (m % 9) / 3, oz = m % 3;
+    const int cell = cell_key(g, t.q.x + ox - 1, t.q.y + oy - 1, t.q.z + oz - 1);
+    if (cell == g.C) continue;
+    if (use_cell(t.bm, ox, oy, oz)) {
+      const int b1 = a.bcs[cell + 1];
+      for (int b = a.bcs[cell]; b < b1; ++b) {
+        const float4 pb = a.bpos[b];
+        const float bx = t.x.x - pb.x, by = t.x.y - pb.y, bz = t.x.z - pb.z;
+        const float d2 = __fmaf_rn(bx, bx, __fmaf_rn(by, by, __fmul_rn(bz, bz)));
+        if (!(d2 > t.Bcut)) push(-b - 1);
+      }
+    }
+    const int j1 = a.cs[cell + 1];
+    for (int j = a.cs[cell]; j < j1; ++j) {
+      const float4 xj = a.xs[j];
+      const float dx = t.x.x - xj.x, dy = t.x.y - xj.y, dz = t.x.z - xj.z;
+      const float rr = t.rc + xj.w;
+      const float d2 = __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmul_rn(dz, dz)));
+      if (!(d2 > rr * rr * 1.0001f) && j != i) push(j);
+    }
+  }
+  flush();
+  a.delta[i] = make_float4(dp.x, dp.y, dp.z, __int_as_float((c & 0xffff) | (s_loc << 16)));
+}
+
 gg_status sweep(gg_system* S, int it, cudaStream_t st) {
   if (S->n <= 0) return GG_OK;
   SweepArgs a;
@@ -556,17 +700,35 @@ gg_status sweep(gg_system* S, int it, cudaStream_t st) {
   a.fcap = S->P.friction_cap;
   a.minr = S->P.boundary_min_radius;
   prof_begin(S, PC_SWEEP, st);
-  // reserved[0] selects a variant for comparison: 0 warp-cooperative
-  // (default), 1 one thread per particle over global memory, 2 shared tile
-  if (S->P.reserved[0] == 1) {
-    auto kern = S->P.math_mode ? k_sweep<1> : k_sweep<0>;
-    kern<<<blocks_for(S->n, 256), 256, 0, st>>>(a);
-  } else if (S->P.reserved[0] == 2) {
-    auto kern = S->P.math_mode ? k_sweep_tiled<1> : k_sweep_tiled<0>;
-    kern<<<blocks_for(S->n, kTileT), kTileT, 0, st>>>(a);
-  } else {
-    auto kern = S->P.math_mode ? k_sweep_warp<1> : k_sweep_warp<0>;
-    kern<<<blocks_for(S->n, kWarpThreads), kWarpThreads, 0, st>>>(a);
+  // reserved[0] selects the sweep variant: 0 warp-cooperative over the
+  // stencil union (default), 1 one thread per particle with pruning,
+  // 2 shared-memory tile, 3 one thread per particle over all 27 cells with
+  // a contact list, 4 warp-cooperative with staged candidates
+  switch (S->P.reserved[0]) {
+    case 1: {
+      auto kern = S->P.math_mode ? k_sweep<1> : k_sweep<0>;
+      kern<<<blocks_for(S->n, 256), 256, 0, st>>>(a);
+      break;
+    }
+    case 2: {
+      auto kern = S->P.math_mode ? k_sweep_tiled<1> : k_sweep_tiled<0>;
+      kern<<<blocks_for(S->n, kTileT), kTileT, 0, st>>>(a);
+      break;
+    }
+    case 3: {
+      auto kern = S->P.math_mode ? k_sweep_list<1> : k_sweep_list<0>;
+      kern<<<blocks_for(S->n, kWarpThreads), kWarpThreads, 0, st>>>(a);
+      break;
+    }
+    case 4: {
+      auto kern = S->P.math_mode ? k_sweep_warp_staged<1> : k_sweep_warp_staged<0>;
+      kern<<<blocks_for(S->n, kWarpThreads), kWarpThreads, 0, st>>>(a);
+      break;
+    }
+    default: {
+      auto kern = S->P.math_mode ? k_sweep_warp_direct<1> : k_sweep_warp_direct<0>;
+      kern<<<blocks_for(S->n, kWarpThreads), kWarpThreads, 0, st>>>(a);
+    }
   }
   count_launches(S, 1);
   prof_end(S, PC_SWEEP, S->n, st);

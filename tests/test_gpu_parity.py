@@ -104,11 +104,10 @@ def test_box_drop_substeps_match_oracle():
     assert s.read(gg.FIELD_CONTACTS).sum() > 0, "the test scene must produce contacts"
 
 
-@pytest.mark.parametrize("variant,other", [(0, 0), (1, 1), (2, 0)])
+@pytest.mark.parametrize("variant,other", [(0, 0), (1, 1), (2, 0), (3, 0), (4, 1)])
 def test_sweep_variants_bit_exact(variant, other):
-    # sweep: warp-cooperative (0), one thread per particle (1), shared tile
-    # (2); surface/distance/merge/upsampling: warp-cooperative (0) or one
-    # thread per particle (1)
+    # sweep variants 0-4 (see kernels_sweep.cu); surface/distance/merge/
+    # upsampling one thread per particle (0) or warp-cooperative (1)
     desc = workloads.box_drop(n_side=16, substeps=4, iters=5, adaptive=1, upsample_per=2)
     desc["params"].reserved[0] = variant
     desc["params"].reserved[1] = other
