@@ -189,6 +189,8 @@ SIGNATURES = {
                                 C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                 C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "gg_grid_destroy": (None, [P_]),
+    "gg_grid_build_noalloc": (C.c_int, [C.c_int32, P_, C.c_int64, C.POINTER(C.c_int32), C.c_float,
+                                        P_, P_, P_, P_]),
     "gg_struct_sizes": (C.c_int, [C.POINTER(C.c_int64), C.c_int32]),
 }
 

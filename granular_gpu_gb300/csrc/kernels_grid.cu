@@ -6,6 +6,7 @@
 //   -> one gather of every SoA field -> cell_start by count + exclusive scan.
 // The sort is stable, as thrust::sort_by_key on int keys is, so the sorted
 // order is identical; it sorts only ceil(log2(C+1)) key bits.
+#include <mutex>
 #include <utility>
 
 #include "common.cuh"
@@ -239,19 +240,11 @@ void sort_scratch_free(SortScratch& s) {
   s.scan_blocks = nullptr;
 }
 
-gg_status grid_sort(const Grid& g, const float4* pos, int64_t n, SortScratch& s, uint32_t* keys_out,
-                    uint32_t* perm_out, uint32_t* keys_unsorted_out, cudaStream_t st, gg_system* prof) {
-  if (n <= 0) return GG_OK;
-  if (n > s.capacity) {
-    set_error("grid_sort: more elements than the sort scratch holds");
-    return GG_ERR_INVALID_ARGUMENT;
-  }
+// Stable LSD sort of the (key, value) pairs held in s.k[0], s.v[0]; the
+// last pass writes keys_out / perm_out.
+static gg_status radix_sort_pairs(const Grid& g, int64_t n, SortScratch& s, uint32_t* keys_out, uint32_t* perm_out,
+                                  cudaStream_t st) {
   const int nn = (int)n;
-  if (prof) prof_begin(prof, PC_HASH, st);
-  k_hash<<<blocks_for(n, 256), 256, 0, st>>>(g, pos, nn, s.k[0], s.v[0], keys_unsorted_out);
-  if (s.counter) *s.counter += 1;
-  if (prof) prof_end(prof, PC_HASH, n, st);
-  if (prof) prof_begin(prof, PC_SORT, st);
   const int bits = key_bits(g.C);
   const int passes = (bits + 7) / 8;
   const int tiles = (int)((n + kSortTile - 1) / kSortTile);
@@ -268,9 +261,26 @@ gg_status grid_sort(const Grid& g, const float4* pos, int64_t n, SortScratch& s,
     if (s.counter) *s.counter += 2;
     src ^= 1;
   }
-  if (prof) prof_end(prof, PC_SORT, n, st);
   GG_CUDA(cudaGetLastError());
   return GG_OK;
+}
+
+gg_status grid_sort(const Grid& g, const float4* pos, int64_t n, SortScratch& s, uint32_t* keys_out,
+                    uint32_t* perm_out, uint32_t* keys_unsorted_out, cudaStream_t st, gg_system* prof) {
+  if (n <= 0) return GG_OK;
+  if (n > s.capacity) {
+    set_error("grid_sort: more elements than the sort scratch holds");
+    return GG_ERR_INVALID_ARGUMENT;
+  }
+  const int nn = (int)n;
+  if (prof) prof_begin(prof, PC_HASH, st);
+  k_hash<<<blocks_for(n, 256), 256, 0, st>>>(g, pos, nn, s.k[0], s.v[0], keys_unsorted_out);
+  if (s.counter) *s.counter += 1;
+  if (prof) prof_end(prof, PC_HASH, n, st);
+  if (prof) prof_begin(prof, PC_SORT, st);
+  gg_status rc = radix_sort_pairs(g, n, s, keys_out, perm_out, st);
+  if (prof) prof_end(prof, PC_SORT, n, st);
+  return rc;
 }
 
 // ------------------------------------------------------------ cell start
@@ -387,4 +397,121 @@ gg_status reorder_upsampled(gg_system* S, const uint32_t* perm, cudaStream_t st)
   return GG_OK;
 }
 
+
+// ------------------------------------------------------------ grid build without allocation
+//
+// gg_grid_build_noalloc: the grid build above (cell keys, stable radix sort,
+// cell start table) for callers that cannot allocate device memory, such as
+// code hosted inside an engine or framework that owns every device
+// allocation, or a loop that must not allocate once it is running.  The
+// caller passes device buffers for the positions and for every output; the
+// sort's scratch (two key/value ping-pong buffers, the per-tile digit
+// histograms and the scan's block sums) lives in the file-scope array below,
+// sized for at most kNoAllocMaxParticles particles and kNoAllocMaxCells
+// cells.  Every GPU that loads this library holds that array (about 4.1 MiB)
+// until the process exits.
+
+constexpr int64_t kNoAllocMaxParticles = 1 << 18;
+constexpr int64_t kNoAllocMaxCells = 1 << 24;
+constexpr int64_t kNoAllocTiles = (kNoAllocMaxParticles + kSortTile - 1) / kSortTile;
+constexpr size_t kNoAllocPairWords = 4 * (size_t)kNoAllocMaxParticles;   // k0, k1, v0, v1
+constexpr size_t kNoAllocHistWords = 256 * (size_t)kNoAllocTiles;
+constexpr size_t kNoAllocScanWords = (size_t)kScanMaxBlocks;
+constexpr size_t kNoAllocWords = kNoAllocPairWords + kNoAllocHistWords + kNoAllocScanWords;
+
+static __device__ __align__(256) uint32_t g_noalloc_scratch[kNoAllocWords];
+
+// mapParticles2Cells_CUDA over packed float[3] positions (12-byte stride).
+__global__ void k_hash3(Grid g, const float* __restrict__ pos3, int n, uint32_t* __restrict__ keys,
+                        uint32_t* __restrict__ vals) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float3 p = make_float3(pos3[3 * i], pos3[3 * i + 1], pos3[3 * i + 2]);
+  const int3 c = floor_cell(g, p);
+  keys[i] = (uint32_t)cell_key(g, c.x, c.y, c.z);
+  vals[i] = (uint32_t)i;
+}
+
+namespace {
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+uint32_t* g_noalloc_dev[kNoAllocMaxDevices] = {};
+
+// The array's name is a host-side stand-in, not a device address: the
+// address is looked up once per device, with that device current.
+gg_status noalloc_scratch(int device, uint32_t** out) {
+  if (device < 0 || device >= kNoAllocMaxDevices) {
+    set_error("gg_grid_build_noalloc: device ordinal out of range");
+    return GG_ERR_INVALID_ARGUMENT;
+  }
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_dev[device]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return cuda_status(e, "gg_grid_build_noalloc: cudaGetSymbolAddress");
+    g_noalloc_dev[device] = (uint32_t*)p;
+  }
+  *out = g_noalloc_dev[device];
+  return GG_OK;
+}
+}  // namespace
+
 }  // namespace gg
+
+extern "C" gg_status gg_grid_build_noalloc(int32_t device, const float* d_pos, int64_t n,
+                                           const int32_t cell_size[3], float cell_length,
+                                           uint32_t* d_sorted_keys, uint32_t* d_perm, int32_t* d_cell_start,
+                                           void* stream) {
+  using namespace gg;
+  try {
+    if (!cell_size || !(cell_length > 0.0f) || n < 0 || (n > 0 && (!d_pos || !d_sorted_keys || !d_perm)) ||
+        !d_cell_start) {
+      set_error("gg_grid_build_noalloc: null buffer or invalid size");
+      return GG_ERR_INVALID_ARGUMENT;
+    }
+    if (cell_size[0] <= 0 || cell_size[1] <= 0 || cell_size[2] <= 0) {
+      set_error("gg_grid_build_noalloc: cell_size must be positive");
+      return GG_ERR_INVALID_ARGUMENT;
+    }
+    const int64_t C = (int64_t)cell_size[0] * cell_size[1] * cell_size[2];
+    if (n > kNoAllocMaxParticles || C > kNoAllocMaxCells) {
+      set_error("gg_grid_build_noalloc: at most 262144 particles and 16777216 cells (static scratch limit); "
+                "use gg_grid_create/gg_grid_build for larger inputs");
+      return GG_ERR_CAPACITY;
+    }
+    GG_CUDA(cudaSetDevice(device));
+    uint32_t* base = nullptr;
+    gg_status rc = noalloc_scratch(device, &base);
+    if (rc != GG_OK) return rc;
+    SortScratch s;
+    s.k[0] = base;
+    s.k[1] = base + kNoAllocMaxParticles;
+    s.v[0] = base + 2 * kNoAllocMaxParticles;
+    s.v[1] = base + 3 * kNoAllocMaxParticles;
+    s.hist = base + kNoAllocPairWords;
+    s.scan_blocks = (int32_t*)(base + kNoAllocPairWords + kNoAllocHistWords);
+    s.capacity = kNoAllocMaxParticles;
+    s.hist_entries = (int64_t)kNoAllocHistWords;
+    s.scan_block_entries = (int64_t)kNoAllocScanWords;
+    Grid g;
+    g.L = cell_length;
+    g.nx = cell_size[0];
+    g.ny = cell_size[1];
+    g.nz = cell_size[2];
+    g.C = (int)C;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (n > 0) {
+      k_hash3<<<blocks_for(n, 256), 256, 0, st>>>(g, d_pos, (int)n, s.k[0], s.v[0]);
+      GG_CUDA(cudaGetLastError());
+      rc = radix_sort_pairs(g, n, s, d_sorted_keys, d_perm, st);
+      if (rc != GG_OK) return rc;
+    }
+    // cell_start_build clears the caller's table (the counts start at zero)
+    // before counting; the histograms and block sums in the scratch are
+    // fully written before they are read, so they need no clearing.
+    return cell_start_build(g, d_sorted_keys, n, d_cell_start, s, st, nullptr);
+  } catch (...) {
+    set_error("gg_grid_build_noalloc: internal error");
+    return GG_ERR_INVALID_ARGUMENT;
+  }
+}

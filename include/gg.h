@@ -283,6 +283,34 @@ gg_status gg_grid_build(gg_grid* g, const float* pos, int64_t n,
                         int32_t* cell_start);
 void gg_grid_destroy(gg_grid* g);
 
+/*
+ * Grid build that allocates nothing.  This entry point has no counterpart in
+ * the reference.  It is for callers that cannot call cudaMalloc: code hosted
+ * in an engine or framework that owns every device allocation through its
+ * own pool, or a loop that must not allocate once it is running.  Such a
+ * caller hands over device buffers it already owns:
+ *   d_pos         n x float[3] positions (device)
+ *   d_sorted_keys n cell keys in stable sorted order (device, written)
+ *   d_perm        n pre-sort indices of the sorted slots (device, written)
+ *   d_cell_start  C+1 cell start offsets, C = product of cell_size (device, written)
+ * The results equal gg_grid_build's.  The sort's scratch memory is a fixed
+ * array inside the library, sized for at most 262,144 particles and
+ * 16,777,216 cells; larger inputs return GG_ERR_CAPACITY with a message.
+ * Every GPU that loads the library keeps that array (about 4.1 MiB) until
+ * the process exits.
+ *   - The first call on a device looks up the array's device address; make
+ *     that first call before any stream capture on that device.
+ *   - Work is queued on `stream` (NULL: the legacy default stream) and the
+ *     call returns without waiting.
+ *   - All calls on a device share the one array: calls whose work overlaps
+ *     on the GPU (other streams, other host threads) race and must be
+ *     serialised by the caller.
+ */
+gg_status gg_grid_build_noalloc(int32_t device, const float* d_pos, int64_t n,
+                                const int32_t cell_size[3], float cell_length,
+                                uint32_t* d_sorted_keys, uint32_t* d_perm,
+                                int32_t* d_cell_start, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
