@@ -111,6 +111,19 @@ def ncu_traffic():
         return None
 
 
+def reduce_over_ranks(ms: float, units: float, device: str = "cuda"):
+    """Replicas: the job takes as long as its slowest rank (max of the
+    timed milliseconds) and processes the units of all ranks (sum)."""
+    import torch
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    u = torch.tensor([float(units)], dtype=torch.float64, device=device)
+    import torch.distributed as tdist
+    if tdist.is_available() and tdist.is_initialized() and tdist.get_world_size() > 1:
+        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+        tdist.all_reduce(u, op=tdist.ReduceOp.SUM)
+    return float(t.item()), float(u.item())
+
+
 def cpu_sample(steps: int, warmup: int, fp64: bool = True):
     """Times the oracle (CPU restatement) on the bounded sample."""
     from granular_gpu_gb300 import workloads
@@ -164,6 +177,7 @@ def run_mine(args):
         desc["params"].math_mode = args.math_mode
     desc["params"].reserved[0] = args.sweep_variant
     desc["params"].reserved[1] = args.stencil_variant
+    desc["params"].nlist_skin = args.nlist_skin * 0.002
     n0 = desc["n_particles"]
     sysg = gg.GranularSystem(**workloads.system_kwargs(desc), device=local)
     stream = torch.cuda.ExternalStream(sysg.stream, device=local)
@@ -194,13 +208,7 @@ def run_mine(args):
     launches = prof.pop("_kernel_launches")
     clocks = sampler.stop()
     ms = ev0.elapsed_time(ev1)
-    t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-    u = torch.tensor([units], dtype=torch.float64, device="cuda")
-    if dist_on:
-        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
-        tdist.all_reduce(u, op=tdist.ReduceOp.SUM)
-    ms_max = float(t.item())
-    total_units = float(u.item())
+    ms_max, total_units = reduce_over_ranks(ms, units)
     value = total_units / (ms_max / 1000.0)
 
     # ---- end to end through the C ABI with pinned host buffers
@@ -242,12 +250,8 @@ def run_mine(args):
         d2h += 2 * hp.nbytes + hu.nbytes
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
-    te = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
-    ue = torch.tensor([e2e_units], dtype=torch.float64, device="cuda")
-    if dist_on:
-        tdist.all_reduce(te, op=tdist.ReduceOp.MAX)
-        tdist.all_reduce(ue, op=tdist.ReduceOp.SUM)
-    e2e_value = float(ue.item()) / float(te.item()) if args.steps_e2e else None
+    e2e_s_max, e2e_total = reduce_over_ranks(e2e_s, e2e_units)
+    e2e_value = e2e_total / e2e_s_max if args.steps_e2e else None
 
     # ---- roofline of the dominant kernel class
     dom = max(prof.items(), key=lambda kv: kv[1]["ms"])
@@ -308,6 +312,8 @@ def main():
     ap.add_argument("--math-mode", type=int, default=0)
     ap.add_argument("--sweep-variant", type=int, default=0,
                     help="0 warp-cooperative, 1 one thread per particle, 2 shared-memory tile")
+    ap.add_argument("--nlist-skin", type=float, default=0.4,
+                    help="contact-list skin in particle radii (sweep variant 5)")
     ap.add_argument("--stencil-variant", type=int, default=0,
                     help="surface/distance/merge/upsampling: 0 warp-cooperative, 1 one thread per particle")
     args = ap.parse_args()

@@ -239,6 +239,10 @@ class GranularSystem:
             out[k] = tuple(out[k])
         return out
 
+    def write_vtk(self, path: str, which: int = SET_UPSAMPLED, swap_yz: bool = True):
+        """ASCII VTK point cloud (the reference's writers, main.cu:190-254)."""
+        _check(lib().gg_write_vtk(self._h, which, path.encode(), int(bool(swap_yz))))
+
     def save(self, path: str):
         _check(lib().gg_save(self._h, path.encode()))
 

@@ -79,7 +79,7 @@ class gg_params(C.Structure):
         ("up_floor_friction", C.c_float), ("up_boundary_damping", C.c_float),
         ("up_ground_band", C.c_float), ("up_ground_damping", C.c_float),
         ("mass_ledger", C.c_int32), ("merge_enabled", C.c_int32),
-        ("upsample_enabled", C.c_int32), ("math_mode", C.c_int32), ("reserved", C.c_int32 * 7),
+        ("upsample_enabled", C.c_int32), ("math_mode", C.c_int32), ("nlist_skin", C.c_float), ("reserved", C.c_int32 * 6),
     ]
 
 
@@ -100,6 +100,7 @@ def default_params() -> gg_params:
     p.up_ground_band, p.up_ground_damping = 0.1, 0.5
     p.mass_ledger, p.merge_enabled, p.upsample_enabled = 0, 1, 1
     p.math_mode = 0
+    p.nlist_skin = 0.0
     return p
 
 
@@ -176,6 +177,7 @@ SIGNATURES = {
     "gg_load": (C.c_int, [P_, C.c_char_p]),
     "gg_stats": (C.c_int, [P_, C.POINTER(gg_stats_t)]),
     "gg_save_particle_stats": (C.c_int, [P_, C.c_char_p]),
+    "gg_write_vtk": (C.c_int, [P_, C.c_int, C.c_char_p, C.c_int32]),
     "gg_set_frame_timing": (C.c_int, [P_, C.c_int32]),
     "gg_frame_times": (C.c_int, [P_, C.POINTER(C.c_float), C.c_int64, C.POINTER(C.c_int64)]),
     "gg_trigger_explosion": (C.c_int, [P_, C.c_float]),

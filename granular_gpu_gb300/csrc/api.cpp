@@ -9,6 +9,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <fstream>
 #include <string>
 #include <vector>
 
@@ -525,6 +526,46 @@ gg_status gg_save_particle_stats(gg_system* S, const char* path) {
             (long long)S->stats_rows[3 * i + 2]);
   }
   fclose(f);
+  return GG_OK;
+  GG_GUARD_END
+}
+
+gg_status gg_write_vtk(gg_system* S, gg_set set, const char* path, int32_t swap_yz) {
+  GG_GUARD_BEGIN
+  REQUIRE(S && path, "gg_write_vtk: null argument");
+  FieldView v;
+  REQUIRE(field_view(S, set, GG_FIELD_POS, v), "gg_write_vtk: unknown set");
+  std::vector<float> p((size_t)std::max<int64_t>(v.count, 1) * 3);
+  GG_CUDA(cudaSetDevice(S->device));
+  GG_CUDA(copy_out(v, p.data(), v.count, S->stream));
+  GG_CUDA(cudaStreamSynchronize(S->stream));
+  std::vector<size_t> keep;
+  keep.reserve((size_t)v.count);
+  for (int64_t i = 0; i < v.count; ++i)
+    if (!std::isnan(p[3 * i]) && !std::isnan(p[3 * i + 1]) && !std::isnan(p[3 * i + 2])) keep.push_back((size_t)i);
+  std::ofstream out(path);
+  if (!out.is_open()) {
+    set_error(std::string("gg_write_vtk: cannot open ") + path);
+    return GG_ERR_IO;
+  }
+  out << "# vtk DataFile Version 3.0\n";
+  out << "Upsampled Granular Particles\n";
+  out << "ASCII\n";
+  out << "DATASET UNSTRUCTURED_GRID\n";
+  out << "POINTS " << keep.size() << " float\n";
+  for (size_t i : keep) {
+    const float x = p[3 * i], y = p[3 * i + 1], z = p[3 * i + 2];
+    if (swap_yz) out << x << " " << z << " " << y << "\n";
+    else out << x << " " << y << " " << z << "\n";
+  }
+  out << "CELLS " << keep.size() << " " << keep.size() * 2 << "\n";
+  for (size_t i = 0; i < keep.size(); ++i) out << "1 " << i << "\n";
+  out << "CELL_TYPES " << keep.size() << "\n";
+  for (size_t i = 0; i < keep.size(); ++i) out << "1\n";
+  if (!out.good()) {
+    set_error(std::string("gg_write_vtk: write failed for ") + path);
+    return GG_ERR_IO;
+  }
   return GG_OK;
   GG_GUARD_END
 }

@@ -35,6 +35,8 @@ struct DevScalars {
 
 enum ErrorBits { ERR_CAPACITY = 1, ERR_NUMERIC = 2, ERR_TIMEOUT = 4 };
 
+constexpr int kNlistMax = 32;  // contact candidates kept per particle
+
 // Kernel classes timed by gg_profile_*.
 enum ProfClass {
   PC_HASH = 0, PC_SORT, PC_REORDER, PC_CELLSTART, PC_PREDICT, PC_SWEEP, PC_APPLY,
@@ -67,6 +69,8 @@ struct Granular {
   int32_t* s_extra = nullptr; // reverse constraint counts delivered by atomics
   int32_t* contacts = nullptr;
   int32_t* ncon = nullptr;
+  int32_t* nl_idx = nullptr;  // contact candidate lists [kNlistMax][cap]
+  int4* nl_meta = nullptr;    // query cell at list build, entry count (-1 = overflow)
   // grid
   uint32_t* keys = nullptr;   // sorted keys of the last build
   uint32_t* perm = nullptr;   // sort permutation of the last build

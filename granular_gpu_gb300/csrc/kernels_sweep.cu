@@ -47,6 +47,11 @@ struct SweepArgs {
   double brad;   // boundary radius (double literal 0.01)
   double fcap;   // friction cap (double literal 0.8)
   float minr;    // floor of the particle radius against walls (0.01f)
+  // contact candidate lists (variant 5)
+  int32_t* __restrict__ nl_idx;
+  int4* __restrict__ nl_meta;
+  int cap;
+  float skin;
 };
 
 // Which of the three cell columns [c-1, c, c+1] along one axis can hold a
@@ -681,6 +686,119 @@ __global__ void __launch_bounds__(kWarpThreads) k_sweep_list(SweepArgs a) {
   a.delta[i] = make_float4(dp.x, dp.y, dp.z, __int_as_float((c & 0xffff) | (s_loc << 16)));
 }
 
+// ------------------------------------------------------------ listed sweep
+//
+// The grid is fixed for all sweeps of a substep and particles move little
+// between sweeps, so each particle keeps the candidates of its stencil that
+// lie within r_i + r_j + skin (walls within 0.01 + r_b + skin), in the
+// reference's order.  A later sweep may use that list instead of scanning
+// while 2 sqrt(3) D < skin, D the largest per-axis displacement summed since
+// the list was built, and while the particle's query cell (hence its
+// stencil) is unchanged: any candidate left out is then still farther than
+// r_i + r_j and cannot be a contact, so the corrections, their order and the
+// counts are exactly those of the full scan.  Every thread replays the same
+// rebuild decision from the device scalars, so no host round trip is needed.
+
+// Sweep index at which the lists in use were built (replayed identically
+// by every thread from the per-sweep displacement bounds).
+__device__ __forceinline__ int nlist_build_sweep(const SweepArgs& a) {
+  int built = 0;
+  float acc = 0.0f;
+  for (int k = 1; k <= a.it; ++k) {
+    acc += __uint_as_float(a.scal->inc_bits[k - 1]);
+    if (!(2.0f * 1.7320509f * acc * 1.0001f < a.skin)) {
+      built = k;
+      acc = 0.0f;
+    }
+  }
+  return built;
+}
+
+template <int MM>
+__device__ __forceinline__ void nlist_apply(const SweepArgs& a, const Target& t, int i, int cnt, float3& dp, int& c,
+                                            int& s_loc) {
+  for (int k = 0; k < cnt; ++k) {
+    const int e = a.nl_idx[(size_t)k * a.cap + i];
+    if (e < 0) {
+      const int b = -e - 1;
+      const float4 pb = a.bpos[b];
+      const float bx = t.x.x - pb.x, by = t.x.y - pb.y, bz = t.x.z - pb.z;
+      const float d2 = __fmaf_rn(bx, bx, __fmaf_rn(by, by, __fmul_rn(bz, bz)));
+      if (d2 > t.Bcut) continue;
+      process_entry<MM>(a, t, i, e, dp, c, s_loc);
+    } else {
+      particle_pair<MM>(a, t, e, a.xs[e], a.inv_m, e, dp, c, s_loc);
+    }
+  }
+}
+
+template <int MM>
+__global__ void __launch_bounds__(256) k_sweep_nlist(SweepArgs a) {
+  const Grid& g = a.g;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  Target t;
+  make_target(a, i, a.xs[i], t);
+  const bool rebuild_all = nlist_build_sweep(a) == a.it;
+  int cnt = -1;
+  if (!rebuild_all) {
+    const int4 m = a.nl_meta[i];
+    if (m.w >= 0 && m.x == t.q.x && m.y == t.q.y && m.z == t.q.z) cnt = m.w;
+  }
+  if (cnt < 0) {
+    // scan the 27 cells in the reference order and keep the candidates
+    // within reach of the skin
+    const float Bs = (float)t.Bd + a.skin;
+    const float Bs2 = Bs * Bs * 1.0001f;
+    int k = 0;
+    bool over = false;
+    for (int m = 0; m < 27 && !over; ++m) {
+      const int ox = m / 9, oy = (m % 9) / 3, oz = m % 3;
+      const int cell = cell_key(g, t.q.x + ox - 1, t.q.y + oy - 1, t.q.z + oz - 1);
+      if (cell == g.C) continue;
+      const int b1 = a.bcs[cell + 1];
+      for (int b = a.bcs[cell]; b < b1; ++b) {
+        const float4 pb = a.bpos[b];
+        const float bx = t.x.x - pb.x, by = t.x.y - pb.y, bz = t.x.z - pb.z;
+        const float d2 = __fmaf_rn(bx, bx, __fmaf_rn(by, by, __fmul_rn(bz, bz)));
+        if (d2 > Bs2) continue;
+        if (k == kNlistMax) {
+          over = true;
+          break;
+        }
+        a.nl_idx[(size_t)k++ * a.cap + i] = -b - 1;
+      }
+      const int j1 = a.cs[cell + 1];
+      for (int j = a.cs[cell]; j < j1 && !over; ++j) {
+        if (j == i) continue;
+        const float4 xj = a.xs[j];
+        const float dx = t.x.x - xj.x, dy = t.x.y - xj.y, dz = t.x.z - xj.z;
+        const float rs = t.rc + xj.w + a.skin;
+        const float d2 = __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmul_rn(dz, dz)));
+        if (d2 > rs * rs * 1.0001f) continue;
+        if (k == kNlistMax) {
+          over = true;
+          break;
+        }
+        a.nl_idx[(size_t)k++ * a.cap + i] = j;
+      }
+    }
+    if (over) {
+      // too many candidates to list: full scan this sweep and every later
+      // sweep of this substep
+      a.nl_meta[i] = make_int4(t.q.x, t.q.y, t.q.z, -1);
+      sweep_global<MM>(a, i, t);
+      return;
+    }
+    a.nl_meta[i] = make_int4(t.q.x, t.q.y, t.q.z, k);
+    cnt = k;
+  }
+  float3 dp = make_float3(0.f, 0.f, 0.f);
+  int c = 0, s_loc = 0;
+  nlist_apply<MM>(a, t, i, cnt, dp, c, s_loc);
+  a.delta[i] = make_float4(dp.x, dp.y, dp.z, __int_as_float((c & 0xffff) | (s_loc << 16)));
+}
+
 gg_status sweep(gg_system* S, int it, cudaStream_t st) {
   if (S->n <= 0) return GG_OK;
   SweepArgs a;
@@ -699,6 +817,10 @@ gg_status sweep(gg_system* S, int it, cudaStream_t st) {
   a.brad = S->P.boundary_radius;
   a.fcap = S->P.friction_cap;
   a.minr = S->P.boundary_min_radius;
+  a.nl_idx = S->g.nl_idx;
+  a.nl_meta = S->g.nl_meta;
+  a.cap = (int)S->cap;
+  a.skin = S->P.nlist_skin;
   prof_begin(S, PC_SWEEP, st);
   // reserved[0] selects the sweep variant: 0 warp-cooperative over the
   // stencil union (default), 1 one thread per particle with pruning,
@@ -718,6 +840,16 @@ gg_status sweep(gg_system* S, int it, cudaStream_t st) {
     case 3: {
       auto kern = S->P.math_mode ? k_sweep_list<1> : k_sweep_list<0>;
       kern<<<blocks_for(S->n, kWarpThreads), kWarpThreads, 0, st>>>(a);
+      break;
+    }
+    case 5: {
+      if (S->g.nl_idx) {
+        auto kern = S->P.math_mode ? k_sweep_nlist<1> : k_sweep_nlist<0>;
+        kern<<<blocks_for(S->n, 256), 256, 0, st>>>(a);
+      } else {
+        auto kern = S->P.math_mode ? k_sweep<1> : k_sweep<0>;
+        kern<<<blocks_for(S->n, 256), 256, 0, st>>>(a);
+      }
       break;
     }
     case 4: {

@@ -120,7 +120,10 @@ typedef struct gg_params {
   int32_t math_mode;           /* 0 = CUDA's cbrtf/expf/norm3df/rsqrtf/acosf, the functions the
                                   reference calls; 1 = each evaluated in double and rounded once
                                   to float (matches the CPU restatement bit for bit) */
-  int32_t reserved[7];
+  float nlist_skin;            /* skin of the per-particle contact lists reused across the sweeps
+                                  of a substep (a length; 0 = scan the stencil every sweep).
+                                  Results do not depend on it, only the speed does. */
+  int32_t reserved[6];
 } gg_params;
 
 /* Arguments of GranularSystem::GranularSystem, GranularSystem.hpp:8-14. */
@@ -249,6 +252,11 @@ gg_status gg_stats(gg_system* sys, gg_stats_t* out);
 /* Solver::save_particle_stats (Solver.cu:1444-1462): writes the per-step
  * "Frame,MergedParticles,SplitParticles,TotalParticles" CSV. */
 gg_status gg_save_particle_stats(gg_system* sys, const char* path);
+
+/* ASCII VTK point cloud of one set's positions, as the reference's writers
+ * produce it (saveFunnelUpsampledPositionsToVTK, main.cu:190-254): NaN
+ * positions are dropped and, with swap_yz, points are written "x z y". */
+gg_status gg_write_vtk(gg_system* sys, gg_set set, const char* path, int32_t swap_yz);
 
 /* GranularSystem::get_frame_times (GranularSystem.hpp:48): per-step device
  * milliseconds, recorded when timing is enabled. */

@@ -118,10 +118,25 @@ def test_sweep_variants_bit_exact(variant, other):
         _compare(s, o, k)
 
 
+@pytest.mark.parametrize("skin", [0.4 * R, 1e-4 * R])
+def test_listed_sweep_bit_exact(skin):
+    # contact lists reused across sweeps; the tiny skin forces rebuilds
+    desc = workloads.box_drop(n_side=16, substeps=4, iters=5, adaptive=1, upsample_per=2)
+    desc["params"].reserved[0] = 5
+    desc["params"].nlist_skin = skin
+    s, o = _pair(desc)
+    for k in range(1, 10):
+        s.step(1)
+        o.step(1)
+        _compare(s, o, k)
+
+
 def test_sweep_column_scene_bit_exact():
     # the benchmark scene's geometry (walls, 2x1x1 box, r = 0.002) at a size
     # the oracle finishes quickly
     desc = workloads.column_collapse(counts=(24, 40, 32), upsample_per=2)
+    desc["params"].reserved[0] = 5
+    desc["params"].nlist_skin = 0.4 * 0.002
     s, o = _pair(desc)
     for k in range(1, 5):
         s.step(1)
@@ -315,3 +330,17 @@ def test_capacity_overflow_matches_oracle_survivors():
     assert s.size() == o.size() == 69
     assert np.array_equal(s.read(gg.FIELD_POS), o.read(abi.FIELD_POS))
     assert np.array_equal(s.read(gg.FIELD_MASS), o.read(abi.FIELD_MASS))
+
+
+def test_vtk_writer(tmp_path):
+    desc = workloads.box_drop(n_side=5, substeps=4, iters=3, upsample_per=2)
+    s = gg.GranularSystem(**workloads.system_kwargs(desc), device=0)
+    path = tmp_path / "frame.vtk"
+    s.write_vtk(str(path))
+    lines = path.read_text().splitlines()
+    n = s.upsampled_size()
+    assert lines[0] == "# vtk DataFile Version 3.0" and lines[4] == f"POINTS {n} float"
+    x = s.read(gg.FIELD_POS, gg.SET_UPSAMPLED)
+    first = [float(v) for v in lines[5].split()]
+    assert np.allclose(first, [x[0, 0], x[0, 2], x[0, 1]], rtol=1e-5)
+    assert lines[5 + n] == f"CELLS {n} {2 * n}" and lines[6 + 2 * n] == f"CELL_TYPES {n}"
