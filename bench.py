@@ -177,7 +177,8 @@ def run_mine(args):
         desc["params"].math_mode = args.math_mode
     desc["params"].reserved[0] = args.sweep_variant
     desc["params"].reserved[1] = args.stencil_variant
-    desc["params"].nlist_skin = args.nlist_skin * 0.002
+    if args.nlist_skin is not None:
+        desc["params"].nlist_skin = args.nlist_skin * 0.002
     n0 = desc["n_particles"]
     sysg = gg.GranularSystem(**workloads.system_kwargs(desc), device=local)
     stream = torch.cuda.ExternalStream(sysg.stream, device=local)
@@ -206,6 +207,7 @@ def run_mine(args):
     barrier()
     prof = sysg.profile_end()
     launches = prof.pop("_kernel_launches")
+    list_builds = prof.pop("_nlist_rebuilds")
     clocks = sampler.stop()
     ms = ev0.elapsed_time(ev1)
     ms_max, total_units = reduce_over_ranks(ms, units)
@@ -280,7 +282,8 @@ def run_mine(args):
         "roofline": {"bound": "hbm", "kernel": "sweep", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                      "algorithmic_bytes_per_particle": SWEEP_BYTES_PER_PARTICLE,
-                     "avg_launch_ms": avg_ms, "dominant_class": dom[0], "shares": shares},
+                     "avg_launch_ms": avg_ms, "dominant_class": dom[0], "shares": shares,
+                     "list_builds_per_particle_sweep": list_builds / max(sweep["units"], 1)},
         "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d // max(args.steps, 1),
                 "d2h_bytes_per_step": d2h // max(args.steps, 1)},
         "gpu_launches": int(launches),
@@ -311,11 +314,14 @@ def main():
                     help="column lattice x,y,z (the benchmark workload is 128,256,256)")
     ap.add_argument("--math-mode", type=int, default=0)
     ap.add_argument("--sweep-variant", type=int, default=0,
-                    help="0 warp-cooperative, 1 one thread per particle, 2 shared-memory tile")
-    ap.add_argument("--nlist-skin", type=float, default=0.4,
-                    help="contact-list skin in particle radii (sweep variant 5)")
+                    help="0 default (contact lists), 1 pruned per particle, 2 shared-memory tile, "
+                         "3 per particle with deferred contacts, 4 warp staged, 5 contact lists, "
+                         "6 warp-cooperative")
+    ap.add_argument("--nlist-skin", type=float, default=None,
+                    help="contact-list skin in radii of 0.002 (default: a tenth of the cell length; "
+                         "0 turns the lists off)")
     ap.add_argument("--stencil-variant", type=int, default=0,
-                    help="surface/distance/merge/upsampling: 0 warp-cooperative, 1 one thread per particle")
+                    help="surface/distance/merge/upsampling: 0 one thread per particle, 1 warp-cooperative")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -270,6 +270,7 @@ class GranularSystem:
             name = bytes(p.names[k]).split(b"\0")[0].decode()
             out[name] = {"launches": p.launches[k], "ms": p.ms[k], "units": p.units[k]}
         out["_kernel_launches"] = p.kernel_launches
+        out["_nlist_rebuilds"] = p.nlist_rebuilds
         return out
 
     @property

@@ -100,7 +100,7 @@ def default_params() -> gg_params:
     p.up_ground_band, p.up_ground_damping = 0.1, 0.5
     p.mass_ledger, p.merge_enabled, p.upsample_enabled = 0, 1, 1
     p.math_mode = 0
-    p.nlist_skin = 0.0
+    p.nlist_skin = -1.0
     return p
 
 
@@ -149,6 +149,7 @@ class gg_profile_t(C.Structure):
         ("n_classes", C.c_int32), ("names", (C.c_char * 24) * GG_PROF_MAX),
         ("launches", C.c_int64 * GG_PROF_MAX), ("ms", C.c_double * GG_PROF_MAX),
         ("units", C.c_int64 * GG_PROF_MAX), ("kernel_launches", C.c_int64),
+        ("nlist_rebuilds", C.c_int64),
     ]
 
 

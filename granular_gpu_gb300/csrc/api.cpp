@@ -113,6 +113,7 @@ gg_status gg_default_params(gg_params* P) {
   P->mass_ledger = 0;
   P->merge_enabled = 1;
   P->upsample_enabled = 1;
+  P->nlist_skin = -1.0f;
   return GG_OK;
 }
 
@@ -609,6 +610,10 @@ gg_status gg_profile_begin(gg_system* S) {
   S->prof_pool_used = 0;
   S->prof_launch_base = S->launches;
   S->profiling = true;
+  if (cudaMemsetAsync(&S->scal->nlist_rebuilds, 0, sizeof(S->scal->nlist_rebuilds), S->stream) != cudaSuccess) {
+    set_error("gg_profile_begin: cannot reset the device counters");
+    return GG_ERR_CUDA;
+  }
   return GG_OK;
 }
 
@@ -620,6 +625,14 @@ gg_status gg_profile_end(gg_system* S, gg_profile_t* out) {
   memset(out, 0, sizeof(*out));
   out->n_classes = PC_COUNT;
   out->kernel_launches = S->launches - S->prof_launch_base;
+  unsigned long long rebuilds = 0;
+  if (cudaMemcpyAsync(&rebuilds, &S->scal->nlist_rebuilds, sizeof(rebuilds), cudaMemcpyDeviceToHost, S->stream) !=
+          cudaSuccess ||
+      cudaStreamSynchronize(S->stream) != cudaSuccess) {
+    set_error("gg_profile_end: cannot read the device counters");
+    return GG_ERR_CUDA;
+  }
+  out->nlist_rebuilds = (int64_t)rebuilds;
   for (int k = 0; k < PC_COUNT && k < GG_PROF_MAX; ++k) {
     strncpy(out->names[k], prof_name(k), 23);
     out->launches[k] = S->prof_launches[k];

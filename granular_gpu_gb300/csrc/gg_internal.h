@@ -31,6 +31,7 @@ struct DevScalars {
   int n_split;
   int n_split_appended;
   int n_kept;
+  unsigned long long nlist_rebuilds;  // listed-sweep list builds (not reset per substep)
 };
 
 enum ErrorBits { ERR_CAPACITY = 1, ERR_NUMERIC = 2, ERR_TIMEOUT = 4 };
@@ -71,6 +72,8 @@ struct Granular {
   int32_t* ncon = nullptr;
   int32_t* nl_idx = nullptr;  // contact candidate lists [kNlistMax][cap]
   int4* nl_meta = nullptr;    // query cell at list build, entry count (-1 = overflow)
+  float* nl_acc = nullptr;    // displacement bound summed since the particle's list build
+  uint32_t* cell_inc = nullptr; // per cell (C+1): max |x* increment| of its particles in the last sweep (float bits)
   // grid
   uint32_t* keys = nullptr;   // sorted keys of the last build
   uint32_t* perm = nullptr;   // sort permutation of the last build
@@ -147,6 +150,7 @@ struct gg_system {
   double* stats_partial = nullptr;     // device FP64 partials
   int stats_blocks = 0;
   int num_sms = 0;
+  float nl_skin = 0.0f;                // contact-list skin in use (0 = lists off)
   int64_t steps = 0;
   int64_t launches = 0;                // kernels launched since create
   int merge_iter = 0;

@@ -81,7 +81,8 @@ gg_status predict(gg_system* S, cudaStream_t st) {
 __global__ void k_apply(int n, float4* __restrict__ xs, float4* __restrict__ pos,
                         const float4* __restrict__ delta, int32_t* __restrict__ s_extra,
                         int32_t* __restrict__ ncon, int32_t* __restrict__ contacts, int stab, int last,
-                        unsigned int* __restrict__ inc_bits) {
+                        unsigned int* __restrict__ inc_bits, const uint32_t* __restrict__ keys,
+                        uint32_t* __restrict__ cell_inc) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   unsigned int bits = 0;
   if (i < n) {
@@ -110,6 +111,9 @@ __global__ void k_apply(int n, float4* __restrict__ xs, float4* __restrict__ pos
       contacts[i] = c;
     }
     bits = __float_as_uint(fmaxf(fmaxf(fabsf(inc.x), fabsf(inc.y)), fabsf(inc.z)));
+    // per-cell bound read by the next listed sweep (non-negative float bits
+    // order like the values; NaN bits are above every finite value)
+    if (cell_inc && bits) atomicMax(&cell_inc[keys[i]], bits);
   }
   warp_max_bits(inc_bits, bits);
 }
@@ -117,9 +121,12 @@ __global__ void k_apply(int n, float4* __restrict__ xs, float4* __restrict__ pos
 gg_status apply(gg_system* S, int it, bool stab, bool last, cudaStream_t st) {
   if (S->n <= 0) return GG_OK;
   prof_begin(S, PC_APPLY, st);
+  // the listed sweep after this one reads the per-cell increments
+  uint32_t* cell_inc = (S->g.cell_inc && !last) ? S->g.cell_inc : nullptr;
+  if (cell_inc) GG_CUDA(cudaMemsetAsync(cell_inc, 0, sizeof(uint32_t) * ((size_t)S->grid.C + 1), st));
   k_apply<<<blocks_for(S->n, 256), 256, 0, st>>>((int)S->n, S->g.xs, S->g.pos[S->g.cur], S->g.delta,
                                                  S->g.s_extra, S->g.ncon, S->g.contacts, stab ? 1 : 0,
-                                                 last ? 1 : 0, &S->scal->inc_bits[it]);
+                                                 last ? 1 : 0, &S->scal->inc_bits[it], S->g.keys, cell_inc);
   count_launches(S, 1);
   prof_end(S, PC_APPLY, S->n, st);
   GG_CUDA(cudaGetLastError());

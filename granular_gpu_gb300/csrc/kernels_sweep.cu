@@ -50,8 +50,11 @@ struct SweepArgs {
   // contact candidate lists (variant 5)
   int32_t* __restrict__ nl_idx;
   int4* __restrict__ nl_meta;
+  float* __restrict__ nl_acc;
+  const uint32_t* __restrict__ cell_inc;
   int cap;
   float skin;
+  float eabs;    // bound on the rounding of one position update
 };
 
 // Which of the three cell columns [c-1, c, c+1] along one axis can hold a
@@ -691,28 +694,20 @@ __global__ void __launch_bounds__(kWarpThreads) k_sweep_list(SweepArgs a) {
 // The grid is fixed for all sweeps of a substep and particles move little
 // between sweeps, so each particle keeps the candidates of its stencil that
 // lie within r_i + r_j + skin (walls within 0.01 + r_b + skin), in the
-// reference's order.  A later sweep may use that list instead of scanning
-// while 2 sqrt(3) D < skin, D the largest per-axis displacement summed since
-// the list was built, and while the particle's query cell (hence its
-// stencil) is unchanged: any candidate left out is then still farther than
-// r_i + r_j and cannot be a contact, so the corrections, their order and the
-// counts are exactly those of the full scan.  Every thread replays the same
-// rebuild decision from the device scalars, so no host round trip is needed.
-
-// Sweep index at which the lists in use were built (replayed identically
-// by every thread from the per-sweep displacement bounds).
-__device__ __forceinline__ int nlist_build_sweep(const SweepArgs& a) {
-  int built = 0;
-  float acc = 0.0f;
-  for (int k = 1; k <= a.it; ++k) {
-    acc += __uint_as_float(a.scal->inc_bits[k - 1]);
-    if (!(2.0f * 1.7320509f * acc * 1.0001f < a.skin)) {
-      built = k;
-      acc = 0.0f;
-    }
-  }
-  return built;
-}
+// reference's order, and runs the contact test on that list only.
+//
+// A list built at sweep t stays exact at sweep s while the particle's query
+// cell (hence its stencil) is unchanged and
+//   sqrt(3) * A * 1.0001 + 4 e < skin,   A = sum over sweeps u in [t, s) of 2 (M_u + e),
+// where M_u bounds the per-axis x* increment of sweep u of the particle and
+// of every particle binned in its stencil, and e bounds the rounding of one
+// position update.  A candidate left out was farther than r_i + r_j + skin
+// and has since closed in by less than the skin, so it is still no contact:
+// the corrections, their order and the counts are those of the full scan.
+// M_u is the sweep's global maximum increment when that is small enough,
+// else the largest per-cell maximum (recorded by the apply kernel) over the
+// 27 stencil cells and the particle's own cell.  Lists whose bound runs out
+// are rebuilt by their own thread; the others are kept.
 
 template <int MM>
 __device__ __forceinline__ void nlist_apply(const SweepArgs& a, const Target& t, int i, int cnt, float3& dp, int& c,
@@ -732,6 +727,27 @@ __device__ __forceinline__ void nlist_apply(const SweepArgs& a, const Target& t,
   }
 }
 
+__device__ __forceinline__ bool nlist_bound_ok(const SweepArgs& a, float A) {
+  return 1.7320509f * A * 1.0001f + 4.0f * a.eabs < a.skin;
+}
+
+// Largest per-cell increment of the last sweep over the stencil of q and the
+// particle's own binning cell.
+__device__ __forceinline__ float nlist_cell_bound(const SweepArgs& a, int3 q, uint32_t own_key) {
+  const Grid& g = a.g;
+  uint32_t m = a.cell_inc[own_key];
+  for (int ox = -1; ox <= 1; ++ox)
+    for (int oy = -1; oy <= 1; ++oy) {
+      const int c0 = cell_key(g, q.x + ox, q.y + oy, q.z - 1);
+      const int c1 = cell_key(g, q.x + ox, q.y + oy, q.z);
+      const int c2 = cell_key(g, q.x + ox, q.y + oy, q.z + 1);
+      if (c0 != g.C) m = max(m, a.cell_inc[c0]);
+      if (c1 != g.C) m = max(m, a.cell_inc[c1]);
+      if (c2 != g.C) m = max(m, a.cell_inc[c2]);
+    }
+  return __uint_as_float(m);
+}
+
 template <int MM>
 __global__ void __launch_bounds__(256) k_sweep_nlist(SweepArgs a) {
   const Grid& g = a.g;
@@ -739,13 +755,24 @@ __global__ void __launch_bounds__(256) k_sweep_nlist(SweepArgs a) {
   if (i >= a.n) return;
   Target t;
   make_target(a, i, a.xs[i], t);
-  const bool rebuild_all = nlist_build_sweep(a) == a.it;
   int cnt = -1;
-  if (!rebuild_all) {
+  if (a.it > 0) {
     const int4 m = a.nl_meta[i];
-    if (m.w >= 0 && m.x == t.q.x && m.y == t.q.y && m.z == t.q.z) cnt = m.w;
+    if (m.w >= 0 && m.x == t.q.x && m.y == t.q.y && m.z == t.q.z) {
+      const float A0 = a.nl_acc[i];
+      float A = A0 + 2.0f * (__uint_as_float(a.scal->inc_bits[a.it - 1]) + a.eabs);
+      if (!nlist_bound_ok(a, A)) A = A0 + 2.0f * (nlist_cell_bound(a, t.q, a.keys[i]) + a.eabs);
+      if (nlist_bound_ok(a, A)) {
+        cnt = m.w;
+        a.nl_acc[i] = A;
+      }
+    }
   }
   if (cnt < 0) {
+    {
+      const unsigned am = __activemask();
+      if ((threadIdx.x & 31) == __ffs(am) - 1) atomicAdd(&a.scal->nlist_rebuilds, (unsigned long long)__popc(am));
+    }
     // scan the 27 cells in the reference order and keep the candidates
     // within reach of the skin
     const float Bs = (float)t.Bd + a.skin;
@@ -784,13 +811,13 @@ __global__ void __launch_bounds__(256) k_sweep_nlist(SweepArgs a) {
       }
     }
     if (over) {
-      // too many candidates to list: full scan this sweep and every later
-      // sweep of this substep
+      // too many candidates to list: full scan, and again at the next sweep
       a.nl_meta[i] = make_int4(t.q.x, t.q.y, t.q.z, -1);
       sweep_global<MM>(a, i, t);
       return;
     }
     a.nl_meta[i] = make_int4(t.q.x, t.q.y, t.q.z, k);
+    a.nl_acc[i] = 0.0f;
     cnt = k;
   }
   float3 dp = make_float3(0.f, 0.f, 0.f);
@@ -819,14 +846,25 @@ gg_status sweep(gg_system* S, int it, cudaStream_t st) {
   a.minr = S->P.boundary_min_radius;
   a.nl_idx = S->g.nl_idx;
   a.nl_meta = S->g.nl_meta;
+  a.nl_acc = S->g.nl_acc;
+  a.cell_inc = S->g.cell_inc;
   a.cap = (int)S->cap;
-  a.skin = S->P.nlist_skin;
+  a.skin = S->nl_skin;
+  {
+    // half an ulp of the largest in-grid coordinate, with a margin
+    const float ext = S->grid.L * (float)std::max(S->grid.nx, std::max(S->grid.ny, S->grid.nz));
+    a.eabs = 2.5e-7f * (1.0f + ext);
+  }
   prof_begin(S, PC_SWEEP, st);
-  // reserved[0] selects the sweep variant: 0 warp-cooperative over the
-  // stencil union (default), 1 one thread per particle with pruning,
-  // 2 shared-memory tile, 3 one thread per particle over all 27 cells with
-  // a contact list, 4 warp-cooperative with staged candidates
-  switch (S->P.reserved[0]) {
+  // reserved[0] selects the sweep variant: 0 (default) contact lists when
+  // they are allocated, else variant 3; 1 one thread per particle with
+  // pruning; 2 shared-memory tile; 3 one thread per particle over all 27
+  // cells with a deferred contact list; 4 warp-cooperative with staged
+  // candidates; 5 contact lists (variant 3 without them); 6 warp-cooperative
+  // over the stencil union
+  int variant = S->P.reserved[0];
+  if (variant == 0 || variant == 5) variant = S->g.nl_idx ? 5 : 3;
+  switch (variant) {
     case 1: {
       auto kern = S->P.math_mode ? k_sweep<1> : k_sweep<0>;
       kern<<<blocks_for(S->n, 256), 256, 0, st>>>(a);
@@ -837,28 +875,23 @@ gg_status sweep(gg_system* S, int it, cudaStream_t st) {
       kern<<<blocks_for(S->n, kTileT), kTileT, 0, st>>>(a);
       break;
     }
-    case 3: {
-      auto kern = S->P.math_mode ? k_sweep_list<1> : k_sweep_list<0>;
-      kern<<<blocks_for(S->n, kWarpThreads), kWarpThreads, 0, st>>>(a);
-      break;
-    }
-    case 5: {
-      if (S->g.nl_idx) {
-        auto kern = S->P.math_mode ? k_sweep_nlist<1> : k_sweep_nlist<0>;
-        kern<<<blocks_for(S->n, 256), 256, 0, st>>>(a);
-      } else {
-        auto kern = S->P.math_mode ? k_sweep<1> : k_sweep<0>;
-        kern<<<blocks_for(S->n, 256), 256, 0, st>>>(a);
-      }
-      break;
-    }
     case 4: {
       auto kern = S->P.math_mode ? k_sweep_warp_staged<1> : k_sweep_warp_staged<0>;
       kern<<<blocks_for(S->n, kWarpThreads), kWarpThreads, 0, st>>>(a);
       break;
     }
-    default: {
+    case 5: {
+      auto kern = S->P.math_mode ? k_sweep_nlist<1> : k_sweep_nlist<0>;
+      kern<<<blocks_for(S->n, 256), 256, 0, st>>>(a);
+      break;
+    }
+    case 6: {
       auto kern = S->P.math_mode ? k_sweep_warp_direct<1> : k_sweep_warp_direct<0>;
+      kern<<<blocks_for(S->n, kWarpThreads), kWarpThreads, 0, st>>>(a);
+      break;
+    }
+    default: {
+      auto kern = S->P.math_mode ? k_sweep_list<1> : k_sweep_list<0>;
       kern<<<blocks_for(S->n, kWarpThreads), kWarpThreads, 0, st>>>(a);
     }
   }

@@ -7,6 +7,7 @@
 // an adaptive step (the reference reads its split count back at the same
 // point, Solver.cu:1162-1163).
 #include <algorithm>
+#include <cmath>
 #include <cstddef>
 #include <cstring>
 
@@ -182,7 +183,7 @@ static void free_all(gg_system* S) {
   }
   void* ptrs[] = {G.merge_vel, G.surface, G.sdist, G.cover, G.xs, G.inv_m, G.delta, G.s_extra, G.contacts,
                   G.ncon, G.keys, G.perm, G.cell_start, G.prop, G.ldens, G.winner, G.split_flag, G.keep_flag,
-                  G.split_slot, G.keep_slot, G.child_pos, G.nl_idx, G.nl_meta, S->b.pos, S->b.animated, S->b.pos_alt,
+                  G.split_slot, G.keep_slot, G.child_pos, G.nl_idx, G.nl_meta, G.nl_acc, G.cell_inc, S->b.pos, S->b.animated, S->b.pos_alt,
                   S->b.animated_alt, S->b.keys, S->b.perm, S->b.cell_start, S->u.keys, S->u.perm, S->scal,
                   S->stats_partial};
   for (void* p : ptrs) cudaFree(p);
@@ -284,9 +285,15 @@ gg_status system_create(const gg_desc* d, gg_system** out) {
   ALLOC(G.cell_start, C1); ALLOC(G.prop, cap); ALLOC(G.ldens, cap); ALLOC(G.winner, cap);
   ALLOC(G.split_flag, cap); ALLOC(G.keep_flag, cap); ALLOC(G.split_slot, cap); ALLOC(G.keep_slot, cap);
   ALLOC(G.child_pos, cap);
-  if (S->P.nlist_skin > 0.0f) {
+  // contact lists: a negative skin asks for the automatic one, a tenth of
+  // the cell length; zero or NaN turns them off
+  S->nl_skin = S->P.nlist_skin < 0.0f ? 0.1f * S->grid.L : S->P.nlist_skin;
+  if (!(S->nl_skin > 0.0f) || !std::isfinite(S->nl_skin)) S->nl_skin = 0.0f;
+  if (S->nl_skin > 0.0f) {
     ALLOC(G.nl_idx, (int64_t)kNlistMax * cap);
     ALLOC(G.nl_meta, cap);
+    ALLOC(G.nl_acc, cap);
+    ALLOC(G.cell_inc, C1);
   }
   ALLOC(S->b.pos, S->nb); ALLOC(S->b.animated, S->nb); ALLOC(S->b.pos_alt, S->nb);
   ALLOC(S->b.animated_alt, S->nb); ALLOC(S->b.keys, S->nb); ALLOC(S->b.perm, S->nb);

@@ -121,8 +121,10 @@ typedef struct gg_params {
                                   reference calls; 1 = each evaluated in double and rounded once
                                   to float (matches the CPU restatement bit for bit) */
   float nlist_skin;            /* skin of the per-particle contact lists reused across the sweeps
-                                  of a substep (a length; 0 = scan the stencil every sweep).
-                                  Results do not depend on it, only the speed does. */
+                                  of a substep: a length; negative (default) = a tenth of the
+                                  cell length; 0 = scan the stencil every sweep.  Results do
+                                  not depend on it, only the speed and memory (148 bytes per
+                                  particle of capacity) do. */
   int32_t reserved[6];
 } gg_params;
 
@@ -190,6 +192,7 @@ typedef struct gg_profile_t {
   double ms[GG_PROF_MAX];
   int64_t units[GG_PROF_MAX];  /* particles (or points) processed, summed over launches */
   int64_t kernel_launches;     /* kernels launched between begin and end */
+  int64_t nlist_rebuilds;      /* contact lists built by listed sweeps (a full stencil scan each) */
 } gg_profile_t;
 
 int32_t gg_abi_version(void);

@@ -104,9 +104,9 @@ def test_box_drop_substeps_match_oracle():
     assert s.read(gg.FIELD_CONTACTS).sum() > 0, "the test scene must produce contacts"
 
 
-@pytest.mark.parametrize("variant,other", [(0, 0), (1, 1), (2, 0), (3, 0), (4, 1)])
+@pytest.mark.parametrize("variant,other", [(0, 0), (1, 1), (2, 0), (3, 0), (4, 1), (6, 0)])
 def test_sweep_variants_bit_exact(variant, other):
-    # sweep variants 0-4 (see kernels_sweep.cu); surface/distance/merge/
+    # sweep variants 0-6 (see kernels_sweep.cu); surface/distance/merge/
     # upsampling one thread per particle (0) or warp-cooperative (1)
     desc = workloads.box_drop(n_side=16, substeps=4, iters=5, adaptive=1, upsample_per=2)
     desc["params"].reserved[0] = variant
@@ -118,17 +118,28 @@ def test_sweep_variants_bit_exact(variant, other):
         _compare(s, o, k)
 
 
-@pytest.mark.parametrize("skin", [0.4 * R, 1e-4 * R])
+@pytest.mark.parametrize("skin", [0.4 * R, 1e-4 * R, 3.0 * R])
 def test_listed_sweep_bit_exact(skin):
-    # contact lists reused across sweeps; the tiny skin forces rebuilds
+    # contact lists reused across sweeps; the tiny skin forces rebuilds and
+    # the large one overflows the lists (full scans)
     desc = workloads.box_drop(n_side=16, substeps=4, iters=5, adaptive=1, upsample_per=2)
     desc["params"].reserved[0] = 5
     desc["params"].nlist_skin = skin
     s, o = _pair(desc)
+    sweeps = desc["params"].stab_iters + desc["params"].iters
+    built = 0
+    scanned = 0
     for k in range(1, 10):
+        n = s.size()
+        s.profile_begin()
         s.step(1)
+        built += s.profile_end()["_nlist_rebuilds"]
+        scanned += n * sweeps
         o.step(1)
         _compare(s, o, k)
+    if skin < R:
+        # every sweep scans with the tiny skin; the usual one keeps lists
+        assert (built == scanned) if skin < 1e-3 * R else (built < scanned / 2)
 
 
 def test_sweep_column_scene_bit_exact():
