@@ -87,13 +87,13 @@ __device__ __forceinline__ unsigned int fbits_abs_max(float a, float b) {
 }
 
 // Warp-aggregated atomicMax of a non-negative float stored as bits.  NaN
-// bits compare above every finite value, so a NaN disables pruning.
+// bits compare above every finite value, so a NaN disables pruning.  The
+// value only grows, so a warp whose maximum does not exceed a value already
+// read skips the atomic: every warp of a large launch would otherwise queue
+// on the same address.
 __device__ __forceinline__ void warp_max_bits(unsigned int* dst, unsigned int v) {
-  for (int o = 16; o > 0; o >>= 1) {
-    unsigned int w = __shfl_xor_sync(0xffffffffu, v, o);
-    v = v > w ? v : w;
-  }
-  if ((threadIdx.x & 31) == 0) atomicMax(dst, v);
+  v = __reduce_max_sync(0xffffffffu, v);
+  if ((threadIdx.x & 31) == 0 && v > __ldcg(dst)) atomicMax(dst, v);
 }
 
 __device__ __forceinline__ unsigned int lanemask_lt() {

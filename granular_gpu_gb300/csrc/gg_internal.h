@@ -25,6 +25,7 @@ struct DevScalars {
   unsigned int inc_bits[64];   // per sweep: max |x* increment| (float bits)
   unsigned int disp0_bits;     // max |dt v| of the predict (float bits)
   unsigned int tile_fallback;  // sweep blocks that could not use the shared-memory tile
+  int nl_queued[64];           // per sweep: particles whose contact list is rebuilt
   int error_word;              // bit0 capacity, bit1 numeric
   int n_after;                 // particle count after the adaptive step
   int n_removed;
@@ -73,6 +74,7 @@ struct Granular {
   int32_t* nl_idx = nullptr;  // contact candidate lists [kNlistMax][cap]
   int4* nl_meta = nullptr;    // query cell at list build, entry count (-1 = overflow)
   float* nl_acc = nullptr;    // displacement bound summed since the particle's list build
+  int32_t* nl_queue = nullptr; // particles whose list is rebuilt in this sweep
   uint32_t* cell_inc = nullptr; // per cell (C+1): max |x* increment| of its particles in the last sweep (float bits)
   // grid
   uint32_t* keys = nullptr;   // sorted keys of the last build

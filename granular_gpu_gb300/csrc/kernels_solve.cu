@@ -85,6 +85,7 @@ __global__ void k_apply(int n, float4* __restrict__ xs, float4* __restrict__ pos
                         uint32_t* __restrict__ cell_inc) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   unsigned int bits = 0;
+  uint32_t key = 0xffffffffu;
   if (i < n) {
     const float4 d = delta[i];
     const int packed = __float_as_int(d.w);
@@ -111,9 +112,15 @@ __global__ void k_apply(int n, float4* __restrict__ xs, float4* __restrict__ pos
       contacts[i] = c;
     }
     bits = __float_as_uint(fmaxf(fmaxf(fabsf(inc.x), fabsf(inc.y)), fabsf(inc.z)));
+    if (cell_inc) key = keys[i];
+  }
+  if (cell_inc) {
     // per-cell bound read by the next listed sweep (non-negative float bits
-    // order like the values; NaN bits are above every finite value)
-    if (cell_inc && bits) atomicMax(&cell_inc[keys[i]], bits);
+    // order like the values; NaN bits are above every finite value); the
+    // lanes of one cell combine first, since sorted neighbours share cells
+    const unsigned peers = __match_any_sync(0xffffffffu, key);
+    const unsigned m = __reduce_max_sync(peers, bits);
+    if (key != 0xffffffffu && m && (threadIdx.x & 31) == __ffs(peers) - 1) atomicMax(&cell_inc[key], m);
   }
   warp_max_bits(inc_bits, bits);
 }

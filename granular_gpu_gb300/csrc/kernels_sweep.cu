@@ -25,6 +25,7 @@
 // ranges (x*, radius, inverse mass) and the cell start offsets into shared
 // memory once, then every thread runs its reference loop from shared memory.
 // Blocks whose union does not fit take the same loop over global memory.
+#include <algorithm>
 #include <climits>
 
 #include "common.cuh"
@@ -51,6 +52,7 @@ struct SweepArgs {
   int32_t* __restrict__ nl_idx;
   int4* __restrict__ nl_meta;
   float* __restrict__ nl_acc;
+  int32_t* __restrict__ nl_queue;
   const uint32_t* __restrict__ cell_inc;
   int cap;
   float skin;
@@ -77,6 +79,8 @@ struct Target {
   float3 x;
   float rc, rb;
   double Bd;      // 0.01 + r_b in double (Solver.cu:283)
+  float Bru;      // Bd rounded up to float: (double)d < Bd  <=>  d < Bru for every float d
+  float capBru;   // (r_b + 0.01) * 0.8 in double, rounded up to float (same use)
   float Bcut;     // conservative float cut for the wall test
   float inv_m;
   int3 q;         // query cell trunc(x*/L)
@@ -85,12 +89,15 @@ struct Target {
   unsigned pm[3], bm[3];
 };
 
-__device__ __forceinline__ void make_target(const SweepArgs& a, int i, float4 xi4, Target& t) {
+// The per-target values every sweep needs (no pruning masks).
+__device__ __forceinline__ void make_target_lite(const SweepArgs& a, int i, float4 xi4, Target& t) {
   const Grid& g = a.g;
   t.x = f3(xi4);
   t.rc = xi4.w;
   t.rb = fmaxf(t.rc, a.minr);
   t.Bd = a.brad + (double)t.rb;
+  t.Bru = __double2float_ru(t.Bd);
+  t.capBru = __double2float_ru(((double)t.rb + a.brad) * a.fcap);
   const float Bf = (float)t.Bd;
   t.Bcut = Bf * Bf * 1.0001f;
   t.inv_m = a.inv_m[i];
@@ -105,13 +112,19 @@ __device__ __forceinline__ void make_target(const SweepArgs& a, int i, float4 xi
     t.cy = r / g.nz;
     t.cz = r - t.cy * g.nz;
   }
+}
+
+// Pruning masks: the stencil columns that can hold a partner within
+// r_i + r_max plus the displacement since binning, or a wall within reach.
+__device__ __forceinline__ void target_masks(const SweepArgs& a, Target& t) {
+  const Grid& g = a.g;
   float disp = __uint_as_float(a.scal->disp0_bits);
   for (int k = 0; k < a.it; ++k) disp += __uint_as_float(a.scal->inc_bits[k]);
   const float rmax = __uint_as_float(a.scal->rmax_bits);
   const float ax = fmaxf(fmaxf(fabsf(t.x.x), fabsf(t.x.y)), fabsf(t.x.z));
   const float slack = 4e-6f * (ax + 1.0f) + 1e-5f * g.L;
   const float Rp = (t.rc + rmax + disp) * 1.0001f + slack;
-  const float Rb = Bf * 1.0001f + slack;
+  const float Rb = (float)t.Bd * 1.0001f + slack;
   t.pm[0] = axis_mask(t.x.x, t.q.x, g.L, Rp);
   t.pm[1] = axis_mask(t.x.y, t.q.y, g.L, Rp);
   t.pm[2] = axis_mask(t.x.z, t.q.z, g.L, Rp);
@@ -120,37 +133,54 @@ __device__ __forceinline__ void make_target(const SweepArgs& a, int i, float4 xi
   t.bm[2] = axis_mask(t.x.z, t.q.z, g.L, Rb);
 }
 
-// boundary_constraint over one cell's wall particles (Solver.cu:272-307).
+__device__ __forceinline__ void make_target(const SweepArgs& a, int i, float4 xi4, Target& t) {
+  make_target_lite(a, i, xi4, t);
+  target_masks(a, t);
+}
+
+// boundary_constraint for one wall particle within the float cut
+// (Solver.cu:272-307).  A float d compares below a double D exactly when it
+// compares below D rounded up to float (no float lies strictly between the
+// two roundings of D), so the double comparisons are decided in float.
+template <int MM>
+__device__ __forceinline__ void wall_contact(const SweepArgs& a, const Target& t, float4 pb, float3& dp, int& c) {
+  const float bx = t.x.x - pb.x, by = t.x.y - pb.y, bz = t.x.z - pb.z;
+  const float dis = m_norm3<MM>(bx, by, bz);
+  if (!(dis < t.Bru)) return;  // mag < 0
+  const float mag = (float)((double)dis - t.Bd);
+  const float3 p12 = make_float3(bx, by, bz);
+  const float3 dpi = smul3(mag / dis, p12);
+  const float3 perp = sub3(dpi, div3s(smul3(dot3(dpi, p12), p12), dis * dis));
+  const float pn = m_norm3<MM>(perp.x, perp.y, perp.z);
+  if (pn < t.capBru) {
+    dp = sub3(dp, dpi);
+  } else {
+    const float minf = (float)fmin((a.brad + (double)t.rb) * a.fcap / (double)pn, 1.0);
+    dp = sub3(dp, mul3s(dpi, minf));
+  }
+  ++c;
+}
+
+__device__ __forceinline__ bool wall_near(const Target& t, float4 pb) {
+  const float bx = t.x.x - pb.x, by = t.x.y - pb.y, bz = t.x.z - pb.z;
+  const float d2 = __fmaf_rn(bx, bx, __fmaf_rn(by, by, __fmul_rn(bz, bz)));
+  return !(d2 > t.Bcut);
+}
+
+// boundary_constraint over one cell's wall particles.
 template <int MM>
 __device__ __forceinline__ void wall_cell(const SweepArgs& a, const Target& t, int cell, float3& dp, int& c) {
   const int b1 = a.bcs[cell + 1];
   for (int b = a.bcs[cell]; b < b1; ++b) {
     const float4 pb = a.bpos[b];
-    const float bx = t.x.x - pb.x, by = t.x.y - pb.y, bz = t.x.z - pb.z;
-    const float d2 = __fmaf_rn(bx, bx, __fmaf_rn(by, by, __fmul_rn(bz, bz)));
-    if (d2 > t.Bcut) continue;
-    const float dis = m_norm3<MM>(bx, by, bz);
-    if (!((double)dis < t.Bd)) continue;  // mag < 0
-    const float mag = (float)((double)dis - t.Bd);
-    const float3 p12 = make_float3(bx, by, bz);
-    const float3 dpi = smul3(mag / dis, p12);
-    const float3 perp = sub3(dpi, div3s(smul3(dot3(dpi, p12), p12), dis * dis));
-    const float pn = m_norm3<MM>(perp.x, perp.y, perp.z);
-    if ((double)pn < ((double)t.rb + a.brad) * a.fcap) {
-      dp = sub3(dp, dpi);
-    } else {
-      const float minf = (float)fmin((a.brad + (double)t.rb) * a.fcap / (double)pn, 1.0);
-      dp = sub3(dp, mul3s(dpi, minf));
-    }
-    ++c;
+    if (wall_near(t, pb)) wall_contact<MM>(a, t, pb, dp, c);
   }
 }
 
 // particles_constraint for one candidate j (Solver.cu:314-357).
-template <int MM>
-__device__ __forceinline__ void particle_pair(const SweepArgs& a, const Target& t, int j, float4 xj4,
-                                              const float* inv_src, int inv_idx, float3& dp, int& c,
-                                              int& s_loc) {
+template <int MM, class InvF>
+__device__ __forceinline__ void particle_pair_f(const SweepArgs& a, const Target& t, int j, float4 xj4, InvF&& inv_of,
+                                                float3& dp, int& c, int& s_loc) {
   const float dx = t.x.x - xj4.x, dy = t.x.y - xj4.y, dz = t.x.z - xj4.z;
   const float rr = t.rc + xj4.w;
   const float d2 = __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmul_rn(dz, dz)));
@@ -158,7 +188,7 @@ __device__ __forceinline__ void particle_pair(const SweepArgs& a, const Target& 
   const float dis = m_norm3<MM>(dx, dy, dz);
   const float mag = rr - dis;
   if (!(mag >= 0.0f)) return;
-  const float inv_mj = inv_src[inv_idx];
+  const float inv_mj = inv_of();
   // (float)(1.0 / (double)s) equals the IEEE float reciprocal of s (no
   // double-rounding case exists for 24-bit significands).
   const float inv_sum = __frcp_rn(t.inv_m + inv_mj);
@@ -198,6 +228,13 @@ __device__ __forceinline__ void particle_pair(const SweepArgs& a, const Target& 
                          llabs((long long)t.cz - qj.z) <= 1;
   if (j_finds_i) ++s_loc;
   else atomicAdd(&a.s_extra[j], 1);
+}
+
+template <int MM>
+__device__ __forceinline__ void particle_pair(const SweepArgs& a, const Target& t, int j, float4 xj4,
+                                              const float* inv_src, int inv_idx, float3& dp, int& c,
+                                              int& s_loc) {
+  particle_pair_f<MM>(a, t, j, xj4, [&]() { return inv_src[inv_idx]; }, dp, c, s_loc);
 }
 
 __device__ __forceinline__ bool use_cell(const unsigned* m, int ox, int oy, int oz) {
@@ -403,23 +440,7 @@ __device__ __forceinline__ void process_entry(const SweepArgs& a, const Target& 
                                               int& c, int& s_loc) {
   if (e < 0) {
     // one wall particle (the exact test of boundary_constraint)
-    const int b = -e - 1;
-    const float4 pb = a.bpos[b];
-    const float bx = t.x.x - pb.x, by = t.x.y - pb.y, bz = t.x.z - pb.z;
-    const float dis = m_norm3<MM>(bx, by, bz);
-    if (!((double)dis < t.Bd)) return;
-    const float mag = (float)((double)dis - t.Bd);
-    const float3 p12 = make_float3(bx, by, bz);
-    const float3 dpi = smul3(mag / dis, p12);
-    const float3 perp = sub3(dpi, div3s(smul3(dot3(dpi, p12), p12), dis * dis));
-    const float pn = m_norm3<MM>(perp.x, perp.y, perp.z);
-    if ((double)pn < ((double)t.rb + a.brad) * a.fcap) {
-      dp = sub3(dp, dpi);
-    } else {
-      const float minf = (float)fmin((a.brad + (double)t.rb) * a.fcap / (double)pn, 1.0);
-      dp = sub3(dp, mul3s(dpi, minf));
-    }
-    ++c;
+    wall_contact<MM>(a, t, a.bpos[-e - 1], dp, c);
   } else {
     particle_pair<MM>(a, t, e, a.xs[e], a.inv_m, e, dp, c, s_loc);
   }
@@ -709,20 +730,38 @@ __global__ void __launch_bounds__(kWarpThreads) k_sweep_list(SweepArgs a) {
 // 27 stencil cells and the particle's own cell.  Lists whose bound runs out
 // are rebuilt by their own thread; the others are kept.
 
-template <int MM>
-__device__ __forceinline__ void nlist_apply(const SweepArgs& a, const Target& t, int i, int cnt, float3& dp, int& c,
-                                            int& s_loc) {
+// The listed candidates in order, with the next entry's gathers issued
+// before the current one is processed.  entry(k) gives the k-th entry: a
+// particle index, or -(wall index) - 1.
+__device__ __forceinline__ void fetch_entry(const SweepArgs& a, int e, float4& p, float& im) {
+  if (e >= 0) {
+    p = a.xs[e];
+    im = a.inv_m[e];
+  } else if (e != INT_MIN) {
+    p = a.bpos[-e - 1];
+  }
+}
+
+template <int MM, class EntryF>
+__device__ __forceinline__ void apply_entries(const SweepArgs& a, const Target& t, int cnt, EntryF&& entry,
+                                              float3& dp, int& c, int& s_loc) {
+  if (cnt <= 0) return;
+  int e_next = entry(0);
+  int e_after = cnt > 1 ? entry(1) : INT_MIN;
+  float4 p_next = make_float4(0.f, 0.f, 0.f, 0.f);
+  float im_next = 0.0f;
+  fetch_entry(a, e_next, p_next, im_next);
   for (int k = 0; k < cnt; ++k) {
-    const int e = a.nl_idx[(size_t)k * a.cap + i];
-    if (e < 0) {
-      const int b = -e - 1;
-      const float4 pb = a.bpos[b];
-      const float bx = t.x.x - pb.x, by = t.x.y - pb.y, bz = t.x.z - pb.z;
-      const float d2 = __fmaf_rn(bx, bx, __fmaf_rn(by, by, __fmul_rn(bz, bz)));
-      if (d2 > t.Bcut) continue;
-      process_entry<MM>(a, t, i, e, dp, c, s_loc);
-    } else {
-      particle_pair<MM>(a, t, e, a.xs[e], a.inv_m, e, dp, c, s_loc);
+    const int e = e_next;
+    const float4 p = p_next;
+    const float im = im_next;
+    e_next = e_after;
+    fetch_entry(a, e_next, p_next, im_next);
+    e_after = (k + 2 < cnt) ? entry(k + 2) : INT_MIN;
+    if (e >= 0) {
+      particle_pair_f<MM>(a, t, e, p, [&]() { return im; }, dp, c, s_loc);
+    } else if (wall_near(t, p)) {
+      wall_contact<MM>(a, t, p, dp, c);
     }
   }
 }
@@ -748,38 +787,77 @@ __device__ __forceinline__ float nlist_cell_bound(const SweepArgs& a, int3 q, ui
   return __uint_as_float(m);
 }
 
+// Sweeps after the first: particles whose list is still exact run it; the
+// others are queued for k_sweep_nlist_build.
 template <int MM>
-__global__ void __launch_bounds__(256) k_sweep_nlist(SweepArgs a) {
+__global__ void __launch_bounds__(256, 4) k_sweep_nlist_keep(SweepArgs a) {
   const Grid& g = a.g;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= a.n) return;
-  Target t;
-  make_target(a, i, a.xs[i], t);
-  int cnt = -1;
-  if (a.it > 0) {
+  bool rebuild = false;
+  if (i < a.n) {
+    const float4 xi4 = a.xs[i];
+    const int3 q = trunc_cell(g, f3(xi4));
     const int4 m = a.nl_meta[i];
-    if (m.w >= 0 && m.x == t.q.x && m.y == t.q.y && m.z == t.q.z) {
+    bool keep = false;
+    if (m.w >= 0 && m.x == q.x && m.y == q.y && m.z == q.z) {
       const float A0 = a.nl_acc[i];
       float A = A0 + 2.0f * (__uint_as_float(a.scal->inc_bits[a.it - 1]) + a.eabs);
-      if (!nlist_bound_ok(a, A)) A = A0 + 2.0f * (nlist_cell_bound(a, t.q, a.keys[i]) + a.eabs);
+      if (!nlist_bound_ok(a, A)) A = A0 + 2.0f * (nlist_cell_bound(a, q, a.keys[i]) + a.eabs);
       if (nlist_bound_ok(a, A)) {
-        cnt = m.w;
+        keep = true;
         a.nl_acc[i] = A;
       }
     }
-  }
-  if (cnt < 0) {
-    {
-      const unsigned am = __activemask();
-      if ((threadIdx.x & 31) == __ffs(am) - 1) atomicAdd(&a.scal->nlist_rebuilds, (unsigned long long)__popc(am));
+    if (keep) {
+      Target t;
+      make_target_lite(a, i, xi4, t);
+      float3 dp = make_float3(0.f, 0.f, 0.f);
+      int c = 0, s_loc = 0;
+      const int32_t* __restrict__ li = a.nl_idx + i;
+      apply_entries<MM>(a, t, m.w, [&](int k) { return __ldcs(li + (size_t)k * a.cap); }, dp, c, s_loc);
+      a.delta[i] = make_float4(dp.x, dp.y, dp.z, __int_as_float((c & 0xffff) | (s_loc << 16)));
+    } else {
+      rebuild = true;
     }
-    // scan the 27 cells in the reference order and keep the candidates
-    // within reach of the skin
+  }
+  const unsigned bal = __ballot_sync(0xffffffffu, rebuild);
+  if (bal) {
+    const int lane = threadIdx.x & 31;
+    int base = 0;
+    if (lane == 0) base = atomicAdd(&a.scal->nl_queued[a.it], __popc(bal));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (rebuild) a.nl_queue[base + __popc(bal & lanemask_lt())] = i;
+  }
+}
+
+// List build: scan the 27 cells in the reference order, keep the candidates
+// within reach of the skin (in shared memory, one column per lane), store
+// the list, then run it.  Every particle at the first sweep of a substep;
+// the queued ones later.
+constexpr int kBuildThreads = 128;
+
+template <int MM>
+__global__ void __launch_bounds__(kBuildThreads) k_sweep_nlist_build(SweepArgs a, int queued) {
+  __shared__ int s_list[kBuildThreads / 32][kNlistMax][32];
+  const Grid& g = a.g;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int total = queued ? a.scal->nl_queued[a.it] : a.n;
+  for (int base = blockIdx.x * kBuildThreads; base < total; base += gridDim.x * kBuildThreads) {
+    const int slot = base + threadIdx.x;
+    const bool act = slot < total;
+    {
+      const unsigned bal = __ballot_sync(0xffffffffu, act);
+      if (lane == 0 && bal) atomicAdd(&a.scal->nlist_rebuilds, (unsigned long long)__popc(bal));
+    }
+    if (!act) continue;
+    const int i = queued ? a.nl_queue[slot] : slot;
+    Target t;
+    make_target_lite(a, i, a.xs[i], t);
     const float Bs = (float)t.Bd + a.skin;
     const float Bs2 = Bs * Bs * 1.0001f;
-    int k = 0;
-    bool over = false;
-    for (int m = 0; m < 27 && !over; ++m) {
+    const float rcs = t.rc + a.skin;
+    int cnt = 0;
+    for (int m = 0; m < 27; ++m) {
       const int ox = m / 9, oy = (m % 9) / 3, oz = m % 3;
       const int cell = cell_key(g, t.q.x + ox - 1, t.q.y + oy - 1, t.q.z + oz - 1);
       if (cell == g.C) continue;
@@ -788,42 +866,38 @@ __global__ void __launch_bounds__(256) k_sweep_nlist(SweepArgs a) {
         const float4 pb = a.bpos[b];
         const float bx = t.x.x - pb.x, by = t.x.y - pb.y, bz = t.x.z - pb.z;
         const float d2 = __fmaf_rn(bx, bx, __fmaf_rn(by, by, __fmul_rn(bz, bz)));
-        if (d2 > Bs2) continue;
-        if (k == kNlistMax) {
-          over = true;
-          break;
+        if (!(d2 > Bs2)) {
+          if (cnt < kNlistMax) s_list[w][cnt][lane] = -b - 1;
+          ++cnt;
         }
-        a.nl_idx[(size_t)k++ * a.cap + i] = -b - 1;
       }
       const int j1 = a.cs[cell + 1];
-      for (int j = a.cs[cell]; j < j1 && !over; ++j) {
-        if (j == i) continue;
+      for (int j = a.cs[cell]; j < j1; ++j) {
         const float4 xj = a.xs[j];
         const float dx = t.x.x - xj.x, dy = t.x.y - xj.y, dz = t.x.z - xj.z;
-        const float rs = t.rc + xj.w + a.skin;
+        const float rs = rcs + xj.w;
         const float d2 = __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmul_rn(dz, dz)));
-        if (d2 > rs * rs * 1.0001f) continue;
-        if (k == kNlistMax) {
-          over = true;
-          break;
+        if (!(d2 > rs * rs * 1.0001f) && j != i) {
+          if (cnt < kNlistMax) s_list[w][cnt][lane] = j;
+          ++cnt;
         }
-        a.nl_idx[(size_t)k++ * a.cap + i] = j;
       }
     }
-    if (over) {
+    if (cnt > kNlistMax) {
       // too many candidates to list: full scan, and again at the next sweep
       a.nl_meta[i] = make_int4(t.q.x, t.q.y, t.q.z, -1);
+      target_masks(a, t);
       sweep_global<MM>(a, i, t);
-      return;
+      continue;
     }
-    a.nl_meta[i] = make_int4(t.q.x, t.q.y, t.q.z, k);
+    for (int k = 0; k < cnt; ++k) a.nl_idx[(size_t)k * a.cap + i] = s_list[w][k][lane];
+    a.nl_meta[i] = make_int4(t.q.x, t.q.y, t.q.z, cnt);
     a.nl_acc[i] = 0.0f;
-    cnt = k;
+    float3 dp = make_float3(0.f, 0.f, 0.f);
+    int c = 0, s_loc = 0;
+    apply_entries<MM>(a, t, cnt, [&](int k) { return s_list[w][k][lane]; }, dp, c, s_loc);
+    a.delta[i] = make_float4(dp.x, dp.y, dp.z, __int_as_float((c & 0xffff) | (s_loc << 16)));
   }
-  float3 dp = make_float3(0.f, 0.f, 0.f);
-  int c = 0, s_loc = 0;
-  nlist_apply<MM>(a, t, i, cnt, dp, c, s_loc);
-  a.delta[i] = make_float4(dp.x, dp.y, dp.z, __int_as_float((c & 0xffff) | (s_loc << 16)));
 }
 
 gg_status sweep(gg_system* S, int it, cudaStream_t st) {
@@ -847,6 +921,7 @@ gg_status sweep(gg_system* S, int it, cudaStream_t st) {
   a.nl_idx = S->g.nl_idx;
   a.nl_meta = S->g.nl_meta;
   a.nl_acc = S->g.nl_acc;
+  a.nl_queue = S->g.nl_queue;
   a.cell_inc = S->g.cell_inc;
   a.cap = (int)S->cap;
   a.skin = S->nl_skin;
@@ -881,8 +956,16 @@ gg_status sweep(gg_system* S, int it, cudaStream_t st) {
       break;
     }
     case 5: {
-      auto kern = S->P.math_mode ? k_sweep_nlist<1> : k_sweep_nlist<0>;
-      kern<<<blocks_for(S->n, 256), 256, 0, st>>>(a);
+      auto build = S->P.math_mode ? k_sweep_nlist_build<1> : k_sweep_nlist_build<0>;
+      if (it == 0) {
+        build<<<blocks_for(S->n, kBuildThreads), kBuildThreads, 0, st>>>(a, 0);
+      } else {
+        auto keep = S->P.math_mode ? k_sweep_nlist_keep<1> : k_sweep_nlist_keep<0>;
+        keep<<<blocks_for(S->n, 256), 256, 0, st>>>(a);
+        const int nb = std::min(blocks_for(S->n, kBuildThreads), S->num_sms * 16);
+        build<<<nb, kBuildThreads, 0, st>>>(a, 1);
+        count_launches(S, 1);
+      }
       break;
     }
     case 6: {

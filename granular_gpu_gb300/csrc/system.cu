@@ -183,7 +183,7 @@ static void free_all(gg_system* S) {
   }
   void* ptrs[] = {G.merge_vel, G.surface, G.sdist, G.cover, G.xs, G.inv_m, G.delta, G.s_extra, G.contacts,
                   G.ncon, G.keys, G.perm, G.cell_start, G.prop, G.ldens, G.winner, G.split_flag, G.keep_flag,
-                  G.split_slot, G.keep_slot, G.child_pos, G.nl_idx, G.nl_meta, G.nl_acc, G.cell_inc, S->b.pos, S->b.animated, S->b.pos_alt,
+                  G.split_slot, G.keep_slot, G.child_pos, G.nl_idx, G.nl_meta, G.nl_acc, G.nl_queue, G.cell_inc, S->b.pos, S->b.animated, S->b.pos_alt,
                   S->b.animated_alt, S->b.keys, S->b.perm, S->b.cell_start, S->u.keys, S->u.perm, S->scal,
                   S->stats_partial};
   for (void* p : ptrs) cudaFree(p);
@@ -293,6 +293,7 @@ gg_status system_create(const gg_desc* d, gg_system** out) {
     ALLOC(G.nl_idx, (int64_t)kNlistMax * cap);
     ALLOC(G.nl_meta, cap);
     ALLOC(G.nl_acc, cap);
+    ALLOC(G.nl_queue, cap);
     ALLOC(G.cell_inc, C1);
   }
   ALLOC(S->b.pos, S->nb); ALLOC(S->b.animated, S->nb); ALLOC(S->b.pos_alt, S->nb);
