@@ -35,6 +35,39 @@ __device__ __forceinline__ int cell_key(const Grid& g, int x, int y, int z) {
              : g.C;
 }
 
+// The 27-cell stencil of q in the reference's order m = 0..26 (dx, dy, dz
+// from -1 to 1, dz fastest), grouped by column: for each (dx, dy) the cells
+// z-1, z, z+1 that lie in the grid have consecutive keys, so f(k0, nc)
+// receives the first key and the number of cells.  The cells skipped are
+// exactly those cell_key maps to C.
+template <class F>
+__device__ __forceinline__ void for_each_stencil_column(const Grid& g, int3 q, F&& f) {
+  const long long zl = max((long long)q.z - 1, 0LL);
+  const long long zh = min((long long)q.z + 1, (long long)g.nz - 1);
+  if (zl > zh) return;
+  for (int ox = -1; ox <= 1; ++ox) {
+    const long long x = (long long)q.x + ox;
+    if (x < 0 || x >= g.nx) continue;
+    for (int oy = -1; oy <= 1; ++oy) {
+      const long long y = (long long)q.y + oy;
+      if (y < 0 || y >= g.ny) continue;
+      f((int)((x * g.ny + y) * g.nz + zl), (int)(zh - zl + 1));
+    }
+  }
+}
+
+// sqrtf(dd) > X, with the clear cases decided from dd against X*X: beyond
+// a relative margin of 2e-6 on the square the rounded root lies several
+// ulps from X.  Near-ties, and X*X outside the normal range, take the root.
+__device__ __forceinline__ bool sqrt_gt(float dd, float X) {
+  const float X2 = X * X;
+  if (X2 > 1e-30f && X2 < 1e30f) {
+    if (dd > X2 * 1.000002f) return true;
+    if (dd < X2 * 0.999998f) return false;
+  }
+  return sqrtf(dd) > X;
+}
+
 // make_int3(pos / cell_length): IEEE division then truncation (cvt.rzi).
 __device__ __forceinline__ int3 trunc_cell(const Grid& g, float3 p) {
   return make_int3(__float2int_rz(p.x / g.L), __float2int_rz(p.y / g.L), __float2int_rz(p.z / g.L));

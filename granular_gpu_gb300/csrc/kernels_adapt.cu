@@ -6,6 +6,8 @@
 // merge_mark_gpu, merge_count_gpu, split_gpu and the DArray compactions and
 // appends (Solver.cu:526-1242, DArray.hpp:62-155).  No allocation and no
 // host round trip except the new particle count.
+#include <cmath>
+
 #include "common.cuh"
 #include "warp_union.cuh"
 
@@ -25,35 +27,32 @@ __global__ void __launch_bounds__(256) k_surface(Grid g, int n, const float4* __
   const float ri = rs[i];
   const int3 q = trunc_cell(g, xi);
   float3 cv = make_float3(0.f, 0.f, 0.f);
-  for (int m = 0; m < 27; ++m) {
-    const int cell = cell_key(g, q.x + m / 9 - 1, q.y + (m % 9) / 3 - 1, q.z + m % 3 - 1);
-    if (cell == g.C) continue;
-    const int j1 = cs[cell + 1];
-    for (int j = cs[cell]; j < j1; ++j) {
+  for_each_stencil_column(g, q, [&](int k0, int nc) {
+    const int j1 = cs[k0 + nc];
+    for (int j = cs[k0]; j < j1; ++j) {
       if (j == i) continue;
       const float3 d = sub3(xi, f3(pos[j]));
-      const float dis = len3(d);
-      if (dis > 2.0f * (ri + rs[j])) continue;
+      if (sqrt_gt(dot3(d, d), 2.0f * (ri + rs[j]))) continue;
       cv = add3(cv, m_normalize3<MM>(d));
     }
-  }
+  });
   const float3 c = m_normalize3<MM>(cv);
   bool vote = false;
   unsigned nn = 0;
-  for (int m = 0; m < 27; ++m) {
-    const int cell = cell_key(g, q.x + m / 9 - 1, q.y + (m % 9) / 3 - 1, q.z + m % 3 - 1);
-    if (cell == g.C) continue;
-    const int j1 = cs[cell + 1];
-    for (int j = cs[cell]; j < j1; ++j) {
+  for_each_stencil_column(g, q, [&](int k0, int nc) {
+    const int j1 = cs[k0 + nc];
+    for (int j = cs[k0]; j < j1; ++j) {
       if (j == i) continue;
       float3 b = sub3(f3(pos[j]), xi);
-      const float dis = len3(b);
-      if (dis > 2.0f * (ri + rs[j])) continue;
-      b = m_normalize3<MM>(b);
-      if (m_acos<MM>(dot3(b, c)) <= cone) vote = true;
+      if (sqrt_gt(dot3(b, b), 2.0f * (ri + rs[j]))) continue;
+      // the vote is an OR: once set, later angles cannot change it
+      if (!vote) {
+        b = m_normalize3<MM>(b);
+        if (m_acos<MM>(dot3(b, c)) <= cone) vote = true;
+      }
       ++nn;
     }
-  }
+  });
   surface[i] = (nn <= (unsigned)min_nb || !vote) ? 1 : 0;
 }
 
@@ -136,17 +135,16 @@ __global__ void __launch_bounds__(256) k_surfdist(Grid g, int n, const float4* _
   const float3 xi = f3(pos[i]);
   const int3 q = trunc_cell(g, xi);
   float best = none;
-  for (int m = 0; m < 27; ++m) {
-    const int cell = cell_key(g, q.x + m / 9 - 1, q.y + (m % 9) / 3 - 1, q.z + m % 3 - 1);
-    if (cell == g.C) continue;
-    const int j1 = cs[cell + 1];
-    for (int j = cs[cell]; j < j1; ++j) {
+  // a minimum: the visiting order does not matter
+  for_each_stencil_column(g, q, [&](int k0, int nc) {
+    const int j1 = cs[k0 + nc];
+    for (int j = cs[k0]; j < j1; ++j) {
       if (j == i || surface[j] == 0) continue;
       const float3 d = sub3(xi, f3(pos[j]));
       const float d2 = dot3(d, d);
       if (d2 < best) best = d2;
     }
-  }
+  });
   sdist[i] = best;
 }
 
@@ -218,6 +216,7 @@ struct MergeArgs {
   float max_mass, min_mass, sdt, target_density;
   double merge_radius;
   float merge_radius_f;  // smallest float above merge_radius: dis < r (double) <=> dis < this
+  float merge_r2_cut;    // smallest float whose sqrtf reaches merge_radius_f: dis < it <=> dd < this
 };
 
 // merge_mark_gpu (Solver.cu:526-653), scan phase: every thread's neighbour
@@ -235,25 +234,28 @@ __global__ void __launch_bounds__(256) k_merge_scan(MergeArgs a) {
   int ci = -1;
   float ld = 0.0f;
   int lc = 0;
-  for (int m = 0; m < 27; ++m) {
-    const int cell = cell_key(a.g, q.x + m / 9 - 1, q.y + (m % 9) / 3 - 1, q.z + m % 3 - 1);
-    if (cell == a.g.C) continue;
-    const int j1 = a.cs[cell + 1];
-    for (int j = a.cs[cell]; j < j1 && j < a.n; ++j) {
-      const float dis = len3(sub3(xi, f3(a.pos[j])));
-      const bool inr = dis < a.merge_radius_f;
+  const bool sd_bug = a.sdist[i] < a.sdt;  // Solver.cu:578 tests [i]: always false here
+  for_each_stencil_column(a.g, q, [&](int k0, int nc) {
+    const int j1 = min(a.cs[k0 + nc], a.n);
+    for (int j = a.cs[k0]; j < j1; ++j) {
+      const float3 d = sub3(xi, f3(a.pos[j]));
+      const float dd = dot3(d, d);
+      // dis < merge radius (as a float) <=> dd below the smallest square
+      // whose rounded root reaches it
+      const bool inr = dd < a.merge_r2_cut;
       if (inr) {
         ld += a.mass[j];
         ++lc;
       }
-      if (j <= i || a.remove[j] != 0 || a.surface[j] != 0 || a.sdist[i] < a.sdt) continue;
+      if (!inr || j <= i || sd_bug || a.remove[j] != 0 || a.surface[j] != 0) continue;
       if (mi + a.mass[j] > a.max_mass) continue;
-      if (inr && dis < closest) {
+      const float dis = sqrtf(dd);
+      if (dis < closest) {
         closest = dis;
         ci = j;
       }
     }
-  }
+  });
   if (lc > 0 && ci != -1) {
     a.prop[i] = ci;
     a.ldens[i] = ld / (float)lc;
@@ -394,6 +396,16 @@ gg_status merge_mark(gg_system* S, cudaStream_t st) {
     a.merge_radius_f = f;
     // dis < r_d  <=>  dis < f when f is the smallest float >= r_d and f != r_d;
     // when f == r_d exactly the comparison is already exact.
+    // sqrtf is correctly rounded and monotone here and on the device, so
+    // sqrtf(dd) < f  <=>  dd < T for the smallest float T with sqrtf(T) >= f.
+    float T = (float)((double)f * (double)f);
+    if (!(f > 0.0f)) T = 0.0f;  // no distance is below it (NaN included)
+    else if (!std::isfinite(T)) T = INFINITY;
+    else {
+      while (T > 0.0f && std::sqrt(nextafterf(T, 0.0f)) >= f) T = nextafterf(T, 0.0f);
+      while (std::sqrt(T) < f) T = nextafterf(T, INFINITY);
+    }
+    a.merge_r2_cut = T;
   }
   const int nb = blocks_for(S->n, 256);
   prof_begin(S, PC_MERGE, st);

@@ -220,11 +220,12 @@ __global__ void __launch_bounds__(256) k_upsample(UpArgs a) {
   float gw = 0.f, maxw = 0.f;
   bool near_b = false;
   const int3 q = floor_cell(g, p);
-  for (int m = 0; m < 27; ++m) {
-    const int cell = cell_key(g, q.x + m / 9 - 1, q.y + (m % 9) / 3 - 1, q.z + m % 3 - 1);
-    if (cell == g.C) continue;
-    const int j1 = a.cs[cell + 1];
-    for (int j = a.cs[cell]; j < j1; ++j) {
+  // The particle sums and the wall sums are separate, so each runs over a
+  // stencil column as one index range (the reference's order within each).
+  for_each_stencil_column(g, q, [&](int k0, int nc) {
+    const int j1 = a.cs[k0 + nc];
+#pragma unroll 2
+    for (int j = a.cs[k0]; j < j1; ++j) {
       const float4 xj = a.gpos[j];
       const float3 d = make_float3(p.x - xj.x, p.y - xj.y, p.z - xj.z);
       const float dd = dot3(d, d);
@@ -237,8 +238,8 @@ __global__ void __launch_bounds__(256) k_upsample(UpArgs a) {
       wv = add3(wv, smul3(w, make_float3(vj.x, vj.y, vj.z)));
       maxw = fmaxf(maxw, w);
     }
-    const int k1 = a.bcs[cell + 1];
-    for (int k = a.bcs[cell]; k < k1; ++k) {
+    const int k1 = a.bcs[k0 + nc];
+    for (int k = a.bcs[k0]; k < k1; ++k) {
       const float4 b = a.bpos[k];
       const float3 tb = make_float3(p.x - b.x, p.y - b.y, p.z - b.z);
       const float dd = dot3(tb, tb);
@@ -251,7 +252,7 @@ __global__ void __launch_bounds__(256) k_upsample(UpArgs a) {
         rep = add3(rep, mul3s(nrm, force));
       }
     }
-  }
+  });
   const float4 uv4 = a.uvel[i];
   const float3 uv = f3(uv4);
   const float3 gdt = make_float3(0.0f * a.dtu, a.gdt_y, 0.0f * a.dtu);

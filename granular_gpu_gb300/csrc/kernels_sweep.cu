@@ -857,32 +857,37 @@ __global__ void __launch_bounds__(kBuildThreads) k_sweep_nlist_build(SweepArgs a
     const float Bs2 = Bs * Bs * 1.0001f;
     const float rcs = t.rc + a.skin;
     int cnt = 0;
-    for (int m = 0; m < 27; ++m) {
-      const int ox = m / 9, oy = (m % 9) / 3, oz = m % 3;
-      const int cell = cell_key(g, t.q.x + ox - 1, t.q.y + oy - 1, t.q.z + oz - 1);
-      if (cell == g.C) continue;
-      const int b1 = a.bcs[cell + 1];
-      for (int b = a.bcs[cell]; b < b1; ++b) {
-        const float4 pb = a.bpos[b];
-        const float bx = t.x.x - pb.x, by = t.x.y - pb.y, bz = t.x.z - pb.z;
-        const float d2 = __fmaf_rn(bx, bx, __fmaf_rn(by, by, __fmul_rn(bz, bz)));
-        if (!(d2 > Bs2)) {
-          if (cnt < kNlistMax) s_list[w][cnt][lane] = -b - 1;
-          ++cnt;
-        }
-      }
-      const int j1 = a.cs[cell + 1];
-      for (int j = a.cs[cell]; j < j1; ++j) {
+    auto push = [&](int e) {
+      if (cnt < kNlistMax) s_list[w][cnt][lane] = e;
+      ++cnt;
+    };
+    auto scan_particles = [&](int j0, int j1) {
+#pragma unroll 4
+      for (int j = j0; j < j1; ++j) {
         const float4 xj = a.xs[j];
         const float dx = t.x.x - xj.x, dy = t.x.y - xj.y, dz = t.x.z - xj.z;
         const float rs = rcs + xj.w;
         const float d2 = __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmul_rn(dz, dz)));
-        if (!(d2 > rs * rs * 1.0001f) && j != i) {
-          if (cnt < kNlistMax) s_list[w][cnt][lane] = j;
-          ++cnt;
-        }
+        if (!(d2 > rs * rs * 1.0001f) && j != i) push(j);
       }
-    }
+    };
+    for_each_stencil_column(g, t.q, [&](int k0, int nc) {
+      if (a.bcs[k0] == a.bcs[k0 + nc]) {
+        // no walls in this column: its particles in index order
+        scan_particles(a.cs[k0], a.cs[k0 + nc]);
+        return;
+      }
+      for (int z = 0; z < nc; ++z) {
+        const int b1 = a.bcs[k0 + z + 1];
+        for (int b = a.bcs[k0 + z]; b < b1; ++b) {
+          const float4 pb = a.bpos[b];
+          const float bx = t.x.x - pb.x, by = t.x.y - pb.y, bz = t.x.z - pb.z;
+          const float d2 = __fmaf_rn(bx, bx, __fmaf_rn(by, by, __fmul_rn(bz, bz)));
+          if (!(d2 > Bs2)) push(-b - 1);
+        }
+        scan_particles(a.cs[k0 + z], a.cs[k0 + z + 1]);
+      }
+    });
     if (cnt > kNlistMax) {
       // too many candidates to list: full scan, and again at the next sweep
       a.nl_meta[i] = make_int4(t.q.x, t.q.y, t.q.z, -1);
