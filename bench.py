@@ -33,9 +33,17 @@ WORKLOAD = "column collapse 128x256x256 (8,388,608 particles, r=0.002, 2x1x1 box
 SAMPLE_COUNTS = (64, 64, 64)
 SAMPLE_NOTE = "64x64x64 sub-lattice (262,144 particles) of the same column scene (same box, grid, walls, " \
               "parameters), one oracle substep per step"
-# algorithmic bytes per particle of one Jacobi iteration: read x* and radius
-# (16 B), write x* (12 B)
-SWEEP_BYTES_PER_PARTICLE = 28
+# Algorithmic (compulsory) bytes per unit of each kernel class, with FP32
+# float3 state and neighbour re-reads assumed to hit in cache: the roofline
+# is reported for whichever class takes the most time in the timed region.
+ALGO_BYTES = {
+    "sweep": (28, "particle", "read x* and radius 16 B, write x* 12 B"),
+    "upsample": (48, "render point", "read render-point position and velocity 24 B, write them 24 B"),
+    "surface": (20, "particle", "read position and radius 16 B, write the surface flag 4 B"),
+    "apply": (56, "particle", "read correction 16 B and x* 12 B, write x* 12 B (stabilisation: x 12 B more), "
+                              "count 4 B"),
+    "merge": (24, "particle", "read position and radius 16 B, surface distance 4 B, write the mark 4 B"),
+}
 
 
 def _dist():
@@ -100,13 +108,15 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
-def ncu_traffic():
-    """Per-launch DRAM bytes of the sweep kernel from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "sweep_traffic.json")
+def ncu_traffic(cls: str):
+    """DRAM bytes per launch of a kernel class from one ncu capture
+    (dram__bytes_read.sum + dram__bytes_write.sum) and the units that launch
+    processed, from the committed summary; None when it has no entry."""
+    path = os.path.join(ROOT, "profiles", "dram_traffic.json")
     try:
         with open(path) as f:
             d = json.load(f)
-        return d
+        return d.get(cls)
     except (OSError, ValueError):
         return None
 
@@ -256,17 +266,20 @@ def run_mine(args):
     e2e_value = e2e_total / e2e_s_max if args.steps_e2e else None
 
     # ---- roofline of the dominant kernel class
-    dom = max(prof.items(), key=lambda kv: kv[1]["ms"])
-    sweep = prof["sweep"]
+    known = {k: v for k, v in prof.items() if k in ALGO_BYTES and v["launches"]}
+    dom = max(known.items(), key=lambda kv: kv[1]["ms"])[0]
+    kp = prof[dom]
+    per_unit, unit_name, byte_note = ALGO_BYTES[dom]
     peak, peak_kind = measured_peak()
-    avg_ms = sweep["ms"] / max(sweep["launches"], 1)
-    units_per_launch = sweep["units"] / max(sweep["launches"], 1)
-    algo_bytes = SWEEP_BYTES_PER_PARTICLE * units_per_launch
+    avg_ms = kp["ms"] / max(kp["launches"], 1)
+    units_per_launch = kp["units"] / max(kp["launches"], 1)
+    algo_bytes = per_unit * units_per_launch
     achieved = algo_bytes / (avg_ms / 1000.0) / 1e9
-    tr = ncu_traffic()
+    tr = ncu_traffic(dom)
     traffic = None
-    if tr and tr.get("particles"):
-        traffic = float(tr["dram_bytes_per_launch"]) * units_per_launch / float(tr["particles"])
+    if tr and tr.get("units"):
+        # traffic grows with the units processed: scale the captured launch
+        traffic = float(tr["dram_bytes"]) * units_per_launch / float(tr["units"])
     total_ms = sum(v["ms"] for v in prof.values())
     shares = {k: round(v["ms"] / total_ms, 4) for k, v in prof.items() if v["launches"]}
 
@@ -279,11 +292,12 @@ def run_mine(args):
                    "boundary": desc["n_boundary"], "cells": int(np.prod(desc["cell_size"])),
                    "l2": "inputs larger than L2 (about 1.9 GB of particle state per step)",
                    "parallelism": f"replicas x{world}"},
-        "roofline": {"bound": "hbm", "kernel": "sweep", "achieved": achieved, "peak": peak, "unit": "GB/s",
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
-                     "algorithmic_bytes_per_particle": SWEEP_BYTES_PER_PARTICLE,
-                     "avg_launch_ms": avg_ms, "dominant_class": dom[0], "shares": shares,
-                     "list_builds_per_particle_sweep": list_builds / max(sweep["units"], 1)},
+                     "algorithmic_bytes_per_unit": per_unit, "unit_of_work": unit_name,
+                     "bytes_basis": byte_note, "units_per_launch": units_per_launch,
+                     "avg_launch_ms": avg_ms, "shares": shares,
+                     "list_builds_per_particle_sweep": list_builds / max(prof["sweep"]["units"], 1)},
         "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d // max(args.steps, 1),
                 "d2h_bytes_per_step": d2h // max(args.steps, 1)},
         "gpu_launches": int(launches),

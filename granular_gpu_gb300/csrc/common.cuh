@@ -129,6 +129,23 @@ __device__ __forceinline__ void warp_max_bits(unsigned int* dst, unsigned int v)
   if ((threadIdx.x & 31) == 0 && v > __ldcg(dst)) atomicMax(dst, v);
 }
 
+// The same for a whole block of kThreads threads (every thread calls it):
+// one fire-and-forget atomic per block, so a large launch puts few
+// requests on the one cache line that holds the maximum.
+template <int kThreads>
+__device__ __forceinline__ void block_max_bits(unsigned int* dst, unsigned int v) {
+  __shared__ unsigned int s_max[kThreads / 32];
+  v = __reduce_max_sync(0xffffffffu, v);
+  if ((threadIdx.x & 31) == 0) s_max[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    unsigned int m = threadIdx.x < kThreads / 32 ? s_max[threadIdx.x] : 0u;
+    m = __reduce_max_sync(0xffffffffu, m);
+    if (threadIdx.x == 0 && m) atomicMax(dst, m);
+  }
+  __syncthreads();  // s_max is reused by the next call
+}
+
 __device__ __forceinline__ unsigned int lanemask_lt() {
   unsigned int m;
   asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));

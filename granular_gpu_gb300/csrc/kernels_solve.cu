@@ -57,8 +57,8 @@ __global__ void k_predict(int n, const float4* __restrict__ pos, const float4* _
     rbits = __float_as_uint(fabsf(p.w));
     dbits = __float_as_uint(fmaxf(fmaxf(fabsf(x.x - p.x), fabsf(x.y - p.y)), fabsf(x.z - p.z)));
   }
-  warp_max_bits(&scal->rmax_bits, rbits);
-  warp_max_bits(&scal->disp0_bits, dbits);
+  block_max_bits<256>(&scal->rmax_bits, rbits);
+  block_max_bits<256>(&scal->disp0_bits, dbits);
 }
 
 gg_status predict(gg_system* S, cudaStream_t st) {
@@ -78,7 +78,7 @@ gg_status predict(gg_system* S, cudaStream_t st) {
 
 // change_position_functor (Solver.cu:403-414): x* += delta / max(1, n); in
 // the stabilisation sweeps x as well (:457-460).
-__global__ void k_apply(int n, float4* __restrict__ xs, float4* __restrict__ pos,
+__global__ void __launch_bounds__(256) k_apply(int n, float4* __restrict__ xs, float4* __restrict__ pos,
                         const float4* __restrict__ delta, int32_t* __restrict__ s_extra,
                         int32_t* __restrict__ ncon, int32_t* __restrict__ contacts, int stab, int last,
                         unsigned int* __restrict__ inc_bits, const uint32_t* __restrict__ keys,
@@ -87,21 +87,24 @@ __global__ void k_apply(int n, float4* __restrict__ xs, float4* __restrict__ pos
   unsigned int bits = 0;
   uint32_t key = 0xffffffffu;
   if (i < n) {
-    const float4 d = delta[i];
+    // every load first, so that they are in flight together
+    const float4 d = __ldcs(&delta[i]);
+    const int se = s_extra[i];
+    float4 x = xs[i];
+    float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (stab) p = pos[i];
+    if (cell_inc) key = keys[i];
     const int packed = __float_as_int(d.w);
     const int c = packed & 0xffff;
     const int sl = (int)((unsigned)packed >> 16);
-    const int se = s_extra[i];
-    s_extra[i] = 0;
     const int nn = c + sl + se;
     const float3 inc = div3s(make_float3(d.x, d.y, d.z), (float)(nn > 1 ? nn : 1));
-    float4 x = xs[i];
+    s_extra[i] = 0;
     x.x = x.x + inc.x;
     x.y = x.y + inc.y;
     x.z = x.z + inc.z;
     xs[i] = x;
     if (stab) {
-      float4 p = pos[i];
       p.x = p.x + inc.x;
       p.y = p.y + inc.y;
       p.z = p.z + inc.z;
@@ -112,7 +115,6 @@ __global__ void k_apply(int n, float4* __restrict__ xs, float4* __restrict__ pos
       contacts[i] = c;
     }
     bits = __float_as_uint(fmaxf(fmaxf(fabsf(inc.x), fabsf(inc.y)), fabsf(inc.z)));
-    if (cell_inc) key = keys[i];
   }
   if (cell_inc) {
     // per-cell bound read by the next listed sweep (non-negative float bits
@@ -122,7 +124,7 @@ __global__ void k_apply(int n, float4* __restrict__ xs, float4* __restrict__ pos
     const unsigned m = __reduce_max_sync(peers, bits);
     if (key != 0xffffffffu && m && (threadIdx.x & 31) == __ffs(peers) - 1) atomicMax(&cell_inc[key], m);
   }
-  warp_max_bits(inc_bits, bits);
+  block_max_bits<256>(inc_bits, bits);
 }
 
 gg_status apply(gg_system* S, int it, bool stab, bool last, cudaStream_t st) {
