@@ -286,18 +286,25 @@ bool field_view(gg_system* S, gg_set set, gg_field f, FieldView& v) {
   return false;
 }
 
-cudaError_t copy_out(const FieldView& v, void* dst, int64_t count, cudaStream_t st) {
+// Device float4 fields cross to the host as packed float[3]: a kernel packs
+// them into the staging buffer and one contiguous copy moves them (a pitched
+// copy with 12-byte rows runs far below the link's bandwidth).
+cudaError_t copy_out(gg_system* S, const FieldView& v, void* dst, int64_t count, cudaStream_t st) {
   if (count <= 0) return cudaSuccess;
   if (v.elem == v.stride)
     return cudaMemcpyAsync(dst, v.ptr, (size_t)v.elem * count, cudaMemcpyDeviceToHost, st);
-  return cudaMemcpy2DAsync(dst, v.elem, v.ptr, v.stride, v.elem, (size_t)count, cudaMemcpyDeviceToHost, st);
+  cudaError_t e = pack3(S, (const float4*)v.ptr, S->stage, count, st);
+  if (e != cudaSuccess) return e;
+  return cudaMemcpyAsync(dst, S->stage, (size_t)12 * count, cudaMemcpyDeviceToHost, st);
 }
 
-cudaError_t copy_in(const FieldView& v, const void* src, int64_t count, cudaStream_t st) {
+cudaError_t copy_in(gg_system* S, const FieldView& v, const void* src, int64_t count, cudaStream_t st) {
   if (count <= 0) return cudaSuccess;
   if (v.elem == v.stride)
     return cudaMemcpyAsync(v.ptr, src, (size_t)v.elem * count, cudaMemcpyHostToDevice, st);
-  return cudaMemcpy2DAsync(v.ptr, v.stride, src, v.elem, v.elem, (size_t)count, cudaMemcpyHostToDevice, st);
+  cudaError_t e = cudaMemcpyAsync(S->stage, src, (size_t)12 * count, cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return e;
+  return unpack3(S, S->stage, (float4*)v.ptr, count, st);
 }
 
 }  // namespace
@@ -311,7 +318,7 @@ gg_status gg_read(gg_system* S, gg_set set, gg_field field, void* host_dst, int6
   if (!host_dst) return GG_OK;
   REQUIRE(capacity >= v.count, "gg_read: destination capacity too small");
   GG_CUDA(cudaSetDevice(S->device));
-  GG_CUDA(copy_out(v, host_dst, v.count, S->stream));
+  GG_CUDA(copy_out(S, v, host_dst, v.count, S->stream));
   GG_CUDA(cudaStreamSynchronize(S->stream));
   return GG_OK;
   GG_GUARD_END
@@ -335,7 +342,7 @@ gg_status gg_write(gg_system* S, gg_set set, gg_field field, const void* host_sr
   REQUIRE(field_view(S, set, field, v), "gg_write: field not available for this set");
   REQUIRE(n == v.count, "gg_write: count must equal the set size");
   GG_CUDA(cudaSetDevice(S->device));
-  GG_CUDA(copy_in(v, host_src, n, S->stream));
+  GG_CUDA(copy_in(S, v, host_src, n, S->stream));
   GG_CUDA(cudaStreamSynchronize(S->stream));
   // positions of the boundary determine its grid
   if (set == GG_SET_BOUNDARY) return boundary_grid(S);
@@ -538,7 +545,7 @@ gg_status gg_write_vtk(gg_system* S, gg_set set, const char* path, int32_t swap_
   REQUIRE(field_view(S, set, GG_FIELD_POS, v), "gg_write_vtk: unknown set");
   std::vector<float> p((size_t)std::max<int64_t>(v.count, 1) * 3);
   GG_CUDA(cudaSetDevice(S->device));
-  GG_CUDA(copy_out(v, p.data(), v.count, S->stream));
+  GG_CUDA(copy_out(S, v, p.data(), v.count, S->stream));
   GG_CUDA(cudaStreamSynchronize(S->stream));
   std::vector<size_t> keep;
   keep.reserve((size_t)v.count);

@@ -150,6 +150,7 @@ struct gg_system {
   gg::DevScalars* scal = nullptr;      // device
   gg::DevScalars* scal_host = nullptr; // pinned mirror
   double* stats_partial = nullptr;     // device FP64 partials
+  float* stage = nullptr;              // device float[3] staging for host copies (max set size)
   int stats_blocks = 0;
   int num_sms = 0;
   float nl_skin = 0.0f;                // contact-list skin in use (0 = lists off)
@@ -234,6 +235,10 @@ gg_status split_and_compact(gg_system* S, cudaStream_t st);
 
 // stats
 gg_status stats_compute(gg_system* S, gg_stats_t* out);
+// float4 <-> packed float[3] through S->stage, so a host copy is one
+// contiguous transfer (the w component on the device is kept).
+cudaError_t pack3(gg_system* S, const float4* src, float* dst, int64_t n, cudaStream_t st);
+cudaError_t unpack3(gg_system* S, const float* src, float4* dst, int64_t n, cudaStream_t st);
 
 // profiling hooks (system.cu)
 void prof_begin(gg_system* S, int cls, cudaStream_t st);

@@ -212,6 +212,14 @@ struct UpArgs {
 
 // update_upsampled_cuda, Solver.cu:1244-1369.  Candidates beyond the kernel
 // support (w = 0 exactly) are skipped; adding +0 would not change a sum.
+//
+// Each stencil column is scanned in chunks of 32 candidates.  A cheap pass
+// (fused multiply-adds, compared with the support radius squared plus a
+// 0.1 % margin) marks the candidates that can carry weight in a 32-bit mask;
+// a second pass evaluates the reference's weight for the marked ones only,
+// in candidate order, so the sums are the reference's.  A warp then spends
+// the weight arithmetic on each lane's own hits instead of on every
+// candidate some lane hits.
 __global__ void __launch_bounds__(256) k_upsample(UpArgs a) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
@@ -226,19 +234,29 @@ __global__ void __launch_bounds__(256) k_upsample(UpArgs a) {
   // stencil column as one index range (the reference's order within each).
   for_each_stencil_column(g, q, [&](int k0, int nc) {
     const int j1 = a.cs[k0 + nc];
-#pragma unroll 2
-    for (int j = a.cs[k0]; j < j1; ++j) {
-      const float4 xj = a.gpos[j];
-      const float3 d = make_float3(p.x - xj.x, p.y - xj.y, p.z - xj.z);
-      const float dd = dot3(d, d);
-      if (dd > a.cut2) continue;
-      const float dis = sqrtf(dd);
-      const float t1 = 1.0f - (dis * dis * a.r9);
-      const float w = fmaxf(0.0f, t1 * t1 * t1);
-      gw += w;
-      const float4 vj = a.gvel[j];
-      wv = add3(wv, smul3(w, make_float3(vj.x, vj.y, vj.z)));
-      maxw = fmaxf(maxw, w);
+    for (int c0 = a.cs[k0]; c0 < j1; c0 += 32) {
+      const int cn = min(32, j1 - c0);
+      unsigned mask = 0u;
+#pragma unroll 4
+      for (int b = 0; b < cn; ++b) {
+        const float4 xj = a.gpos[c0 + b];
+        const float dx = p.x - xj.x, dy = p.y - xj.y, dz = p.z - xj.z;
+        const float dd = __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmul_rn(dz, dz)));
+        mask |= (dd <= a.cut2 ? 1u : 0u) << b;
+      }
+      while (mask) {
+        const int j = c0 + __ffs(mask) - 1;
+        mask &= mask - 1u;
+        const float4 xj = a.gpos[j];
+        const float3 d = make_float3(p.x - xj.x, p.y - xj.y, p.z - xj.z);
+        const float dis = sqrtf(dot3(d, d));
+        const float t1 = 1.0f - (dis * dis * a.r9);
+        const float w = fmaxf(0.0f, t1 * t1 * t1);
+        gw += w;
+        const float4 vj = a.gvel[j];
+        wv = add3(wv, smul3(w, make_float3(vj.x, vj.y, vj.z)));
+        maxw = fmaxf(maxw, w);
+      }
     }
     const int k1 = a.bcs[k0 + nc];
     for (int k = a.bcs[k0]; k < k1; ++k) {

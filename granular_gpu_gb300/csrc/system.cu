@@ -185,7 +185,7 @@ static void free_all(gg_system* S) {
                   G.ncon, G.keys, G.perm, G.cell_start, G.prop, G.ldens, G.winner, G.split_flag, G.keep_flag,
                   G.split_slot, G.keep_slot, G.child_pos, G.nl_idx, G.nl_meta, G.nl_acc, G.nl_queue, G.cell_inc, S->b.pos, S->b.animated, S->b.pos_alt,
                   S->b.animated_alt, S->b.keys, S->b.perm, S->b.cell_start, S->u.keys, S->u.perm, S->scal,
-                  S->stats_partial};
+                  S->stats_partial, S->stage};
   for (void* p : ptrs) cudaFree(p);
   if (S->scal_host) cudaFreeHost(S->scal_host);
   sort_scratch_free(S->sort);
@@ -303,6 +303,7 @@ gg_status system_create(const gg_desc* d, gg_system** out) {
   ALLOC(S->scal, 1);
   S->stats_blocks = std::max(1, std::min(4 * S->num_sms, 1024));
   ALLOC(S->stats_partial, (int64_t)S->stats_blocks * 16);
+  ALLOC(S->stage, 3 * std::max<int64_t>(std::max(cap, S->nu), S->nb));
 #undef ALLOC
   if (e == cudaSuccess) e = cudaMallocHost((void**)&S->scal_host, sizeof(DevScalars));
   if (e != cudaSuccess) {
@@ -497,6 +498,63 @@ gg_status stats_compute(gg_system* S, gg_stats_t* out) {
   out->max_penetration = pen;
   out->error_word = S->error_word;
   return GG_OK;
+}
+
+}  // namespace gg
+
+// ------------------------------------------------------------ host copies
+
+namespace gg {
+
+constexpr int kPackThreads = 256;
+
+// float4 -> packed float[3]: each block stages its 256 elements in shared
+// memory and writes them back as 768 consecutive floats (coalesced).
+__global__ void __launch_bounds__(kPackThreads) k_pack3(const float4* __restrict__ src, float* __restrict__ dst,
+                                                         int64_t n) {
+  __shared__ float s[3 * kPackThreads];
+  const int64_t base = (int64_t)blockIdx.x * kPackThreads;
+  const int t = threadIdx.x;
+  if (base + t < n) {
+    const float4 v = src[base + t];
+    s[3 * t] = v.x;
+    s[3 * t + 1] = v.y;
+    s[3 * t + 2] = v.z;
+  }
+  __syncthreads();
+  const int cnt = 3 * (int)(n - base < kPackThreads ? n - base : kPackThreads);
+  for (int k = t; k < cnt; k += kPackThreads) dst[3 * base + k] = s[k];
+}
+
+__global__ void __launch_bounds__(kPackThreads) k_unpack3(const float* __restrict__ src, float4* __restrict__ dst,
+                                                           int64_t n) {
+  __shared__ float s[3 * kPackThreads];
+  const int64_t base = (int64_t)blockIdx.x * kPackThreads;
+  const int t = threadIdx.x;
+  const int cnt = 3 * (int)(n - base < kPackThreads ? n - base : kPackThreads);
+  for (int k = t; k < cnt; k += kPackThreads) s[k] = src[3 * base + k];
+  __syncthreads();
+  if (base + t < n) {
+    float4 v = dst[base + t];
+    v.x = s[3 * t];
+    v.y = s[3 * t + 1];
+    v.z = s[3 * t + 2];
+    dst[base + t] = v;
+  }
+}
+
+cudaError_t pack3(gg_system* S, const float4* src, float* dst, int64_t n, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  k_pack3<<<(unsigned)((n + kPackThreads - 1) / kPackThreads), kPackThreads, 0, st>>>(src, dst, n);
+  count_launches(S, 1);
+  return cudaGetLastError();
+}
+
+cudaError_t unpack3(gg_system* S, const float* src, float4* dst, int64_t n, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  k_unpack3<<<(unsigned)((n + kPackThreads - 1) / kPackThreads), kPackThreads, 0, st>>>(src, dst, n);
+  count_launches(S, 1);
+  return cudaGetLastError();
 }
 
 }  // namespace gg
