@@ -17,7 +17,7 @@ from .abi import (FIELD_ADAPTIVE_LAST_STEP, FIELD_CELL_KEY, FIELD_CELL_START,  #
                   FIELD_POS, FIELD_REMOVE, FIELD_SURFACE, FIELD_SURFACE_DISTANCE, FIELD_VEL,
                   SET_BOUNDARY, SET_GRANULAR, SET_UPSAMPLED, default_params)
 
-__all__ = ["GranularSystem", "GranularError", "Grid", "scene_build", "default_params", "lib"]
+__all__ = ["GranularSystem", "GranularError", "Grid", "Mlp", "scene_build", "default_params", "lib"]
 
 _LIB = None
 
@@ -346,6 +346,74 @@ class Grid:
     def close(self):
         if getattr(self, "_h", None):
             lib().gg_grid_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _dptr(t):
+    """Device address of a torch CUDA tensor (or an int address)."""
+    if t is None:
+        return None
+    if isinstance(t, int):
+        return C.c_void_p(t)
+    return C.c_void_p(t.data_ptr())
+
+
+class Mlp:
+    """The warm-start network (gg_mlp_*): 48 -> 64 -> 64 -> 3, ReLU, BF16
+    tensor-core kernels with FP32 accumulation.  Feature and target arrays
+    are device memory (torch CUDA tensors or raw addresses): features n x 48
+    bf16, targets n x 3 float32."""
+
+    N_FEATURES, N_HIDDEN, N_OUT = 48, 64, 3
+
+    def __init__(self, device: int = 0, seed: int = 1):
+        self.device = device
+        h = C.c_void_p()
+        _check(lib().gg_mlp_create(device, seed, C.byref(h)))
+        self._h = h
+
+    @staticmethod
+    def num_params() -> int:
+        return int(lib().gg_mlp_num_params())
+
+    @property
+    def handle(self):
+        return self._h
+
+    def get_params(self) -> np.ndarray:
+        out = np.zeros(self.num_params(), np.float32)
+        _check(lib().gg_mlp_get_params(self._h, _fptr(out), out.size))
+        return out
+
+    def set_params(self, params):
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        _check(lib().gg_mlp_set_params(self._h, _fptr(p), p.size))
+
+    def forward(self, features, out, n: int, stream=None):
+        _check(lib().gg_mlp_forward(self._h, _dptr(features), n, _dptr(out), stream))
+
+    def gradient(self, features, targets, n: int, stream=None):
+        g = np.zeros(self.num_params(), np.float32)
+        loss = C.c_float()
+        _check(lib().gg_mlp_gradient(self._h, _dptr(features), _dptr(targets), n, _fptr(g), C.byref(loss),
+                                     stream))
+        return g, float(loss.value)
+
+    def train_step(self, features, targets, n: int, lr: float, weight_decay: float = 0.0, stream=None) -> float:
+        loss = C.c_float()
+        _check(lib().gg_mlp_train_step(self._h, _dptr(features), _dptr(targets), n, lr, weight_decay,
+                                       C.byref(loss), stream))
+        return float(loss.value)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().gg_mlp_destroy(self._h)
             self._h = None
 
     def __del__(self):

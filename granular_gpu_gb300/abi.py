@@ -195,6 +195,14 @@ SIGNATURES = {
     "gg_grid_build_noalloc": (C.c_int, [C.c_int32, P_, C.c_int64, C.POINTER(C.c_int32), C.c_float,
                                         P_, P_, P_, P_]),
     "gg_struct_sizes": (C.c_int, [C.POINTER(C.c_int64), C.c_int32]),
+    "gg_mlp_create": (C.c_int, [C.c_int32, C.c_uint64, C.POINTER(P_)]),
+    "gg_mlp_num_params": (C.c_int64, []),
+    "gg_mlp_set_params": (C.c_int, [P_, C.POINTER(C.c_float), C.c_int64]),
+    "gg_mlp_get_params": (C.c_int, [P_, C.POINTER(C.c_float), C.c_int64]),
+    "gg_mlp_forward": (C.c_int, [P_, P_, C.c_int64, P_, P_]),
+    "gg_mlp_gradient": (C.c_int, [P_, P_, P_, C.c_int64, C.POINTER(C.c_float), C.POINTER(C.c_float), P_]),
+    "gg_mlp_train_step": (C.c_int, [P_, P_, P_, C.c_int64, C.c_float, C.c_float, C.POINTER(C.c_float), P_]),
+    "gg_mlp_destroy": (None, [P_]),
 }
 
 PKG_DIR = os.path.dirname(os.path.abspath(__file__))

@@ -322,6 +322,32 @@ gg_status gg_grid_build_noalloc(int32_t device, const float* d_pos, int64_t n,
                                 uint32_t* d_sorted_keys, uint32_t* d_perm,
                                 int32_t* d_cell_start, void* stream);
 
+/*
+ * Learned warm start.  No counterpart in the reference: a 48 -> 64 -> 64 -> 3
+ * MLP (ReLU, BF16 weights on the tensor cores, FP32 accumulation) that
+ * predicts a substep's Jacobi position correction from per-particle
+ * neighbourhood features (gg_params.warm_start).  Feature and target
+ * buffers are device memory: features n x 48 bf16 row-major (16-byte
+ * aligned), targets and outputs n x 3 float, in units of |g| dt^2.
+ */
+typedef struct gg_mlp gg_mlp;
+/* He-uniform initial weights from `seed`, zero biases. */
+gg_status gg_mlp_create(int32_t device, uint64_t seed, gg_mlp** out);
+/* Parameters as one fp32 vector: W1[48][64] b1[64] W2[64][64] b2[64] W3[64][3] b3[3]. */
+int64_t gg_mlp_num_params(void);
+gg_status gg_mlp_set_params(gg_mlp* mlp, const float* host_params, int64_t n);
+gg_status gg_mlp_get_params(gg_mlp* mlp, float* host_params, int64_t n);
+/* Prediction for n feature rows; waits for the result. */
+gg_status gg_mlp_forward(gg_mlp* mlp, const void* d_features, int64_t n, float* d_out, void* stream);
+/* Mean squared error over n samples and its gradient (same layout as the
+ * parameters), copied to host buffers (either may be NULL). */
+gg_status gg_mlp_gradient(gg_mlp* mlp, const void* d_features, const float* d_targets, int64_t n,
+                          float* host_grad, float* host_loss, void* stream);
+/* One Adam step (beta 0.9/0.999) on the gradient of n samples. */
+gg_status gg_mlp_train_step(gg_mlp* mlp, const void* d_features, const float* d_targets, int64_t n, float lr,
+                            float weight_decay, float* host_loss, void* stream);
+void gg_mlp_destroy(gg_mlp* mlp);
+
 #ifdef __cplusplus
 }
 #endif
