@@ -12,7 +12,7 @@ import numpy as np
 
 from . import abi
 from .abi import (FIELD_ADAPTIVE_LAST_STEP, FIELD_CELL_KEY, FIELD_CELL_START,  # noqa: F401
-                  FIELD_CONTACTS, FIELD_IS_ANIMATED, FIELD_MASS, FIELD_MASS_UNITS, FIELD_MERGE,
+                  FIELD_CONTACTS, FIELD_FEATURES, FIELD_IS_ANIMATED, FIELD_WARM_TARGET, FIELD_MASS, FIELD_MASS_UNITS, FIELD_MERGE,
                   FIELD_MERGE_COUNT, FIELD_MERGE_VELOCITY, FIELD_NUM_CONSTRAINTS, FIELD_PERM,
                   FIELD_POS, FIELD_REMOVE, FIELD_SURFACE, FIELD_SURFACE_DISTANCE, FIELD_VEL,
                   SET_BOUNDARY, SET_GRANULAR, SET_UPSAMPLED, default_params)
@@ -229,6 +229,24 @@ class GranularSystem:
         p, n, st = C.c_void_p(), C.c_int64(), C.c_int32()
         _check(lib().gg_device_ptr(self._h, which, field, C.byref(p), C.byref(n), C.byref(st)))
         return p.value, n.value, st.value
+
+    @property
+    def params(self) -> "abi.gg_params":
+        """A copy of the parameters in use (gg_get_params)."""
+        p = abi.gg_params()
+        _check(lib().gg_get_params(self._h, C.byref(p)))
+        return p
+
+    @params.setter
+    def params(self, p):
+        _check(lib().gg_set_params(self._h, C.byref(p)))
+
+    # -- learned warm start -------------------------------------------------
+    def set_warm_start(self, mlp=None):
+        """gg_set_warm_start: attach a network (gg_params.warm_start = 1) or,
+        with None, only allocate the buffers of the recording mode (2)."""
+        _check(lib().gg_set_warm_start(self._h, mlp.handle if mlp is not None else None))
+        self._mlp = mlp
 
     # -- diagnostics, snapshots, timing ----------------------------------
     def stats(self) -> dict:

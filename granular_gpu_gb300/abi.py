@@ -43,6 +43,8 @@ FIELD_ADAPTIVE_LAST_STEP = 13
 FIELD_IS_ANIMATED = 14
 FIELD_CONTACTS = 15
 FIELD_NUM_CONSTRAINTS = 16
+FIELD_FEATURES = 17
+FIELD_WARM_TARGET = 18
 
 # (numpy dtype name, components) of each field
 FIELD_LAYOUT = {
@@ -54,7 +56,8 @@ FIELD_LAYOUT = {
     FIELD_MERGE: ("float32", 1), FIELD_MERGE_COUNT: ("int32", 1),
     FIELD_MERGE_VELOCITY: ("float32", 3), FIELD_ADAPTIVE_LAST_STEP: ("int32", 1),
     FIELD_IS_ANIMATED: ("int32", 1), FIELD_CONTACTS: ("int32", 1),
-    FIELD_NUM_CONSTRAINTS: ("int32", 1),
+    FIELD_NUM_CONSTRAINTS: ("int32", 1), FIELD_FEATURES: ("uint16", 48),
+    FIELD_WARM_TARGET: ("float32", 3),
 }
 
 UNITS_PER_MASS = 1 << 20
@@ -79,7 +82,9 @@ class gg_params(C.Structure):
         ("up_floor_friction", C.c_float), ("up_boundary_damping", C.c_float),
         ("up_ground_band", C.c_float), ("up_ground_damping", C.c_float),
         ("mass_ledger", C.c_int32), ("merge_enabled", C.c_int32),
-        ("upsample_enabled", C.c_int32), ("math_mode", C.c_int32), ("nlist_skin", C.c_float), ("reserved", C.c_int32 * 6),
+        ("upsample_enabled", C.c_int32), ("math_mode", C.c_int32), ("nlist_skin", C.c_float),
+        ("target_residual", C.c_float), ("max_sweeps", C.c_int32), ("warm_start", C.c_int32),
+        ("warm_start_scale", C.c_float), ("reserved", C.c_int32 * 2),
     ]
 
 
@@ -101,6 +106,7 @@ def default_params() -> gg_params:
     p.mass_ledger, p.merge_enabled, p.upsample_enabled = 0, 1, 1
     p.math_mode = 0
     p.nlist_skin = -1.0
+    p.target_residual, p.max_sweeps, p.warm_start, p.warm_start_scale = 0.0, 200, 0, 1.0
     return p
 
 
@@ -138,6 +144,8 @@ class gg_stats_t(C.Structure):
         ("momentum", C.c_double * 3), ("kinetic_energy", C.c_double),
         ("center_of_mass", C.c_double * 3), ("max_penetration", C.c_float),
         ("nonfinite", C.c_int32), ("error_word", C.c_int32), ("launches", C.c_int64),
+        ("last_sweeps", C.c_int32), ("last_residual", C.c_float), ("last_residual_max", C.c_float),
+        ("pad_", C.c_int32),
     ]
 
 
@@ -203,6 +211,9 @@ SIGNATURES = {
     "gg_mlp_gradient": (C.c_int, [P_, P_, P_, C.c_int64, C.POINTER(C.c_float), C.POINTER(C.c_float), P_]),
     "gg_mlp_train_step": (C.c_int, [P_, P_, P_, C.c_int64, C.c_float, C.c_float, C.POINTER(C.c_float), P_]),
     "gg_mlp_destroy": (None, [P_]),
+    "gg_set_warm_start": (C.c_int, [P_, P_]),
+    "gg_get_params": (C.c_int, [P_, C.POINTER(gg_params)]),
+    "gg_set_params": (C.c_int, [P_, C.POINTER(gg_params)]),
 }
 
 PKG_DIR = os.path.dirname(os.path.abspath(__file__))

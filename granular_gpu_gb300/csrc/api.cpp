@@ -114,6 +114,10 @@ gg_status gg_default_params(gg_params* P) {
   P->merge_enabled = 1;
   P->upsample_enabled = 1;
   P->nlist_skin = -1.0f;
+  P->target_residual = 0.0f;
+  P->max_sweeps = 200;
+  P->warm_start = 0;
+  P->warm_start_scale = 1.0f;
   return GG_OK;
 }
 
@@ -259,6 +263,12 @@ bool field_view(gg_system* S, gg_set set, gg_field f, FieldView& v) {
       case GG_FIELD_ADAPTIVE_LAST_STEP: v.ptr = G.als[c]; return true;
       case GG_FIELD_CONTACTS: v.ptr = G.contacts; return true;
       case GG_FIELD_NUM_CONSTRAINTS: v.ptr = G.ncon; return true;
+      case GG_FIELD_FEATURES:
+        if (!S->feat) return false;
+        v.ptr = S->feat; v.elem = 96; v.stride = 96; return true;
+      case GG_FIELD_WARM_TARGET:
+        if (!S->warm_target) return false;
+        v.ptr = S->warm_target; v.elem = 12; v.stride = 12; return true;
       default: return false;
     }
   }
@@ -308,6 +318,23 @@ cudaError_t copy_in(gg_system* S, const FieldView& v, const void* src, int64_t c
 }
 
 }  // namespace
+
+gg_status gg_get_params(gg_system* S, gg_params* out) {
+  REQUIRE(S && out, "gg_get_params: null argument");
+  *out = S->P;
+  return GG_OK;
+}
+
+gg_status gg_set_params(gg_system* S, const gg_params* P) {
+  REQUIRE(S && P, "gg_set_params: null argument");
+  if (!(P->nlist_skin == S->P.nlist_skin || (std::isnan(P->nlist_skin) && std::isnan(S->P.nlist_skin)))) {
+    set_error("gg_set_params: nlist_skin cannot change after gg_create");
+    return GG_ERR_NOT_SUPPORTED;
+  }
+  REQUIRE(P->stab_iters >= 0 && P->iters >= 0 && P->max_sweeps >= 0, "gg_set_params: negative sweep count");
+  S->P = *P;
+  return GG_OK;
+}
 
 gg_status gg_read(gg_system* S, gg_set set, gg_field field, void* host_dst, int64_t capacity, int64_t* n) {
   GG_GUARD_BEGIN

@@ -22,10 +22,13 @@ struct Grid {
 // Scalars that live on the device so a substep needs no host round trip.
 struct DevScalars {
   unsigned int rmax_bits;      // max contact radius (float bits), this step
-  unsigned int inc_bits[64];   // per sweep: max |x* increment| (float bits)
+  unsigned int inc_bits[256];  // per sweep: max |x* increment| (float bits)
   unsigned int disp0_bits;     // max |dt v| of the predict (float bits)
   unsigned int tile_fallback;  // sweep blocks that could not use the shared-memory tile
-  int nl_queued[64];           // per sweep: particles whose contact list is rebuilt
+  int nl_queued[256];          // per sweep: particles whose contact list is rebuilt
+  unsigned int pen_bits;       // residual mode: largest penetration (float bits)
+  unsigned int pen_count;      // residual mode: contacts (particle pairs counted once per side, walls)
+  double pen_sum;              // residual mode: sum of their penetrations
   int error_word;              // bit0 capacity, bit1 numeric
   int n_after;                 // particle count after the adaptive step
   int n_removed;
@@ -35,6 +38,8 @@ struct DevScalars {
   unsigned long long nlist_rebuilds;  // listed-sweep list builds (not reset per substep)
 };
 
+constexpr int kMaxSweeps = 256;  // sweeps per substep (stabilisation + Jacobi)
+
 enum ErrorBits { ERR_CAPACITY = 1, ERR_NUMERIC = 2, ERR_TIMEOUT = 4 };
 
 constexpr int kNlistMax = 32;  // contact candidates kept per particle
@@ -43,7 +48,7 @@ constexpr int kNlistMax = 32;  // contact candidates kept per particle
 enum ProfClass {
   PC_HASH = 0, PC_SORT, PC_REORDER, PC_CELLSTART, PC_PREDICT, PC_SWEEP, PC_APPLY,
   PC_FINALIZE, PC_UPSAMPLE, PC_UP_GRID, PC_SURFACE, PC_SURFDIST, PC_MERGE, PC_SPLIT,
-  PC_COMPACT, PC_STATS, PC_COUNT
+  PC_COMPACT, PC_STATS, PC_FEATURES, PC_MLP, PC_RESIDUAL, PC_COUNT
 };
 
 // Double-buffered particle SoA; index `cur` is the live copy.
@@ -151,6 +156,14 @@ struct gg_system {
   gg::DevScalars* scal_host = nullptr; // pinned mirror
   double* stats_partial = nullptr;     // device FP64 partials
   float* stage = nullptr;              // device float[3] staging for host copies (max set size)
+  // learned warm start (allocated by gg_set_warm_start)
+  gg_mlp* mlp = nullptr;               // attached network (not owned)
+  void* feat = nullptr;                // cap x 48 bf16 features of the last substep
+  float4* xs0 = nullptr;               // cap: x* after the predict (warm_start = 2)
+  float* warm_target = nullptr;        // cap x 3: (x*_final - x*_predict) / (|g| dt^2)
+  int32_t last_sweeps = 0;
+  float last_residual = 0.0f;         // mean penetration over contacts
+  float last_residual_max = 0.0f;     // largest penetration
   int stats_blocks = 0;
   int num_sms = 0;
   float nl_skin = 0.0f;                // contact-list skin in use (0 = lists off)
@@ -232,6 +245,11 @@ gg_status surface_distance(gg_system* S, cudaStream_t st);
 gg_status merge_mark(gg_system* S, cudaStream_t st);
 gg_status merge_count(gg_system* S, cudaStream_t st);
 gg_status split_and_compact(gg_system* S, cudaStream_t st);
+// learned warm start and residual-targeted sweeps (kernels_learn.cu)
+gg_status warm_start_apply(gg_system* S, cudaStream_t st);
+gg_status warm_start_record(gg_system* S, cudaStream_t st);
+gg_status warm_start_target(gg_system* S, cudaStream_t st);
+gg_status residual(gg_system* S, cudaStream_t st, float* out);
 
 // stats
 gg_status stats_compute(gg_system* S, gg_stats_t* out);

@@ -18,6 +18,8 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstddef>
+#include <cstring>
 #include <mutex>
 
 #include "common.cuh"
@@ -981,3 +983,223 @@ void gg_mlp_destroy(gg_mlp* M) {
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------ in the substep
+
+namespace gg {
+
+namespace {
+
+// Length and velocity scales of the features and the prediction: |g| dt^2
+// and |g| dt (a tenth of the cell length per substep without gravity).
+void warm_scales(const gg_system* S, float& slen, float& svel) {
+  const double g = std::sqrt((double)S->phys.g.x * S->phys.g.x + (double)S->phys.g.y * S->phys.g.y +
+                             (double)S->phys.g.z * S->phys.g.z);
+  const double dt = S->phys.dt;
+  slen = (float)(g * dt * dt);
+  svel = (float)(g * dt);
+  if (!(slen > 0.0f) || !(svel > 0.0f)) {
+    slen = 0.1f * S->grid.L;
+    svel = slen / (float)(dt > 0 ? dt : 1.0);
+  }
+}
+
+gg_status features(gg_system* S, cudaStream_t st) {
+  if (S->n <= 0) return GG_OK;
+  const int c = S->g.cur;
+  float slen, svel;
+  warm_scales(S, slen, svel);
+  FeatArgs a;
+  a.g = S->grid;
+  a.n = (int)S->n;
+  a.xs = S->g.xs;
+  a.pos = S->g.pos[c];
+  a.vel = S->g.vel[c];
+  a.mass = S->g.mass[c];
+  a.cs = S->g.cell_start;
+  a.bcs = S->b.cell_start;
+  a.bpos = S->b.pos;
+  a.out = reinterpret_cast<__nv_bfloat16*>(S->feat);
+  a.inv_slen = 1.0f / slen;
+  a.inv_svel = 1.0f / svel;
+  a.brad = (float)S->P.boundary_radius;
+  a.minr = S->P.boundary_min_radius;
+  a.inv_height = 1.0f / (S->grid.L * (float)S->grid.ny);
+  prof_begin(S, PC_FEATURES, st);
+  k_features<<<blocks_for(S->n, 256), 256, 0, st>>>(a);
+  count_launches(S, 1);
+  prof_end(S, PC_FEATURES, S->n, st);
+  GG_CUDA(cudaGetLastError());
+  return GG_OK;
+}
+
+__global__ void k_warm_target(int n, const float4* __restrict__ xs, const float4* __restrict__ xs0,
+                              float* __restrict__ target, float inv_slen) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4 a = xs[i], b = xs0[i];
+  target[3 * (size_t)i] = (a.x - b.x) * inv_slen;
+  target[3 * (size_t)i + 1] = (a.y - b.y) * inv_slen;
+  target[3 * (size_t)i + 2] = (a.z - b.z) * inv_slen;
+}
+
+// Penetration at x*, r_i + r_j - |x_i - x_j| over the particle pairs in the
+// sweeps' stencil and (0.01 + max(r_i, 0.01)) - |x - b| over wall
+// particles: the largest, and the sum and number of the positive ones (a
+// pair counts once from each side; the mean is unchanged by that).
+__global__ void __launch_bounds__(256) k_residual(Grid g, int n, const float4* __restrict__ xs,
+                                                  const int32_t* __restrict__ cs, const int32_t* __restrict__ bcs,
+                                                  const float4* __restrict__ bpos, float brad, float minr,
+                                                  DevScalars* __restrict__ scal) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  float best = 0.0f, sum = 0.0f;
+  unsigned int cnt = 0;
+  if (i < n) {
+    const float4 x4 = xs[i];
+    const float3 x = f3(x4);
+    const float ri = x4.w;
+    const float Bw = brad + fmaxf(ri, minr);
+    const int3 q = trunc_cell(g, x);
+    for_each_stencil_column(g, q, [&](int k0, int nc) {
+      const int j1 = cs[k0 + nc];
+      for (int j = cs[k0]; j < j1; ++j) {
+        if (j == i) continue;
+        const float4 xj = xs[j];
+        const float dx = x.x - xj.x, dy = x.y - xj.y, dz = x.z - xj.z;
+        const float R = ri + xj.w;
+        const float d2 = dx * dx + dy * dy + dz * dz;
+        if (d2 < R * R) {
+          const float p = R - sqrtf(d2);
+          best = fmaxf(best, p);
+          sum += p;
+          ++cnt;
+        }
+      }
+      const int b1 = bcs[k0 + nc];
+      for (int b = bcs[k0]; b < b1; ++b) {
+        const float4 pb = bpos[b];
+        const float dx = x.x - pb.x, dy = x.y - pb.y, dz = x.z - pb.z;
+        const float d2 = dx * dx + dy * dy + dz * dz;
+        if (d2 < Bw * Bw) {
+          const float p = Bw - sqrtf(d2);
+          best = fmaxf(best, p);
+          sum += p;
+          ++cnt;
+        }
+      }
+    });
+  }
+  __shared__ float s_sum[8];
+  __shared__ unsigned int s_cnt[8];
+  float ws = sum;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) ws += __shfl_xor_sync(0xffffffffu, ws, o);
+  const unsigned int wc = __reduce_add_sync(0xffffffffu, cnt);
+  if ((threadIdx.x & 31) == 0) {
+    s_sum[threadIdx.x >> 5] = ws;
+    s_cnt[threadIdx.x >> 5] = wc;
+  }
+  block_max_bits<256>(&scal->pen_bits, __float_as_uint(best));  // synchronises the block
+  if (threadIdx.x == 0) {
+    double bs = 0.0;
+    unsigned int bc = 0;
+    for (int w = 0; w < 8; ++w) {
+      bs += (double)s_sum[w];
+      bc += s_cnt[w];
+    }
+    if (bc) {
+      atomicAdd(&scal->pen_sum, bs);
+      atomicAdd(&scal->pen_count, bc);
+    }
+  }
+}
+
+}  // namespace
+
+gg_status warm_start_apply(gg_system* S, cudaStream_t st) {
+  if (!S->mlp || !S->feat) {
+    set_error("warm_start = 1 needs a network attached with gg_set_warm_start");
+    return GG_ERR_INVALID_ARGUMENT;
+  }
+  if (S->n <= 0) return GG_OK;
+  gg_status rc = features(S, st);
+  if (rc != GG_OK) return rc;
+  float slen, svel;
+  warm_scales(S, slen, svel);
+  prof_begin(S, PC_MLP, st);
+  rc = mlp_forward(S->mlp, S->feat, S->n, nullptr, S->g.xs, S->g.pos[S->g.cur], slen * S->P.warm_start_scale,
+                   &S->scal->disp0_bits, st, &S->launches);
+  prof_end(S, PC_MLP, S->n, st);
+  return rc;
+}
+
+gg_status warm_start_record(gg_system* S, cudaStream_t st) {
+  if (!S->feat) {
+    set_error("warm_start = 2 needs gg_set_warm_start (it allocates the buffers)");
+    return GG_ERR_INVALID_ARGUMENT;
+  }
+  if (S->n <= 0) return GG_OK;
+  gg_status rc = features(S, st);
+  if (rc != GG_OK) return rc;
+  GG_CUDA(cudaMemcpyAsync(S->xs0, S->g.xs, sizeof(float4) * (size_t)S->n, cudaMemcpyDeviceToDevice, st));
+  return GG_OK;
+}
+
+gg_status warm_start_target(gg_system* S, cudaStream_t st) {
+  if (S->n <= 0) return GG_OK;
+  float slen, svel;
+  warm_scales(S, slen, svel);
+  k_warm_target<<<blocks_for(S->n, 256), 256, 0, st>>>((int)S->n, S->g.xs, S->xs0, S->warm_target, 1.0f / slen);
+  count_launches(S, 1);
+  GG_CUDA(cudaGetLastError());
+  return GG_OK;
+}
+
+gg_status residual(gg_system* S, cudaStream_t st, float* out) {
+  *out = 0.0f;
+  S->last_residual_max = 0.0f;
+  if (S->n <= 0) return GG_OK;
+  const size_t off = offsetof(DevScalars, pen_bits);
+  const size_t len = offsetof(DevScalars, pen_sum) + sizeof(double) - off;
+  GG_CUDA(cudaMemsetAsync(reinterpret_cast<char*>(S->scal) + off, 0, len, st));
+  prof_begin(S, PC_RESIDUAL, st);
+  k_residual<<<blocks_for(S->n, 256), 256, 0, st>>>(S->grid, (int)S->n, S->g.xs, S->g.cell_start, S->b.cell_start,
+                                                    S->b.pos, (float)S->P.boundary_radius,
+                                                    S->P.boundary_min_radius, S->scal);
+  count_launches(S, 1);
+  prof_end(S, PC_RESIDUAL, S->n, st);
+  GG_CUDA(cudaGetLastError());
+  GG_CUDA(cudaMemcpyAsync(reinterpret_cast<char*>(S->scal_host) + off, reinterpret_cast<char*>(S->scal) + off, len,
+                          cudaMemcpyDeviceToHost, st));
+  GG_CUDA(cudaStreamSynchronize(st));
+  std::memcpy(&S->last_residual_max, &S->scal_host->pen_bits, sizeof(float));
+  const unsigned int c = S->scal_host->pen_count;
+  *out = c ? (float)(S->scal_host->pen_sum / (double)c) : 0.0f;
+  return GG_OK;
+}
+
+}  // namespace gg
+
+extern "C" gg_status gg_set_warm_start(gg_system* S, gg_mlp* M) {
+  if (!S) {
+    set_error("gg_set_warm_start: null system");
+    return GG_ERR_INVALID_ARGUMENT;
+  }
+  if (M && M->device != S->device) {
+    set_error("gg_set_warm_start: the network lives on another device");
+    return GG_ERR_INVALID_ARGUMENT;
+  }
+  GG_CUDA(cudaSetDevice(S->device));
+  const size_t cap = (size_t)std::max<int64_t>(S->cap, 1);
+  cudaError_t e = cudaSuccess;
+  if (!S->feat) e = cudaMalloc(&S->feat, cap * kFeat * 2);
+  if (e == cudaSuccess && !S->xs0) e = cudaMalloc((void**)&S->xs0, cap * sizeof(float4));
+  if (e == cudaSuccess && !S->warm_target) e = cudaMalloc((void**)&S->warm_target, cap * 3 * sizeof(float));
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    set_error(std::string("gg_set_warm_start: allocation failed: ") + cudaGetErrorString(e));
+    return GG_ERR_OUT_OF_MEMORY;
+  }
+  S->mlp = M;
+  return GG_OK;
+}

@@ -67,7 +67,8 @@ void prof_flush(gg_system* S) {
 const char* prof_name(int cls) {
   static const char* kNames[PC_COUNT] = {"hash", "sort", "reorder", "cell_start", "predict", "sweep",
                                          "apply", "finalize", "upsample", "up_grid", "surface",
-                                         "surf_dist", "merge", "split", "compact", "stats"};
+                                         "surf_dist", "merge", "split", "compact", "stats",
+                                         "features", "mlp", "residual"};
   return (cls >= 0 && cls < PC_COUNT) ? kNames[cls] : "?";
 }
 
@@ -121,11 +122,36 @@ gg_status step_once(gg_system* S) {
   if ((rc = upsampled_grid(S)) != GG_OK) return rc;
   // Solver::step, Solver.cu:82-109
   if ((rc = predict(S, st)) != GG_OK) return rc;
-  const int total = S->P.stab_iters + S->P.iters;
-  for (int it = 0; it < total; ++it) {
-    if ((rc = sweep(S, it, st)) != GG_OK) return rc;
-    if ((rc = apply(S, it, it < S->P.stab_iters, it == total - 1, st)) != GG_OK) return rc;
+  if (S->P.warm_start == 1 && (rc = warm_start_apply(S, st)) != GG_OK) return rc;
+  if (S->P.warm_start == 2 && (rc = warm_start_record(S, st)) != GG_OK) return rc;
+  if (S->P.target_residual > 0.0f) {
+    // residual mode: the stabilisation sweeps, then Jacobi sweeps until the
+    // largest penetration, measured before each sweep, is within the target
+    const int stab = S->P.stab_iters;
+    for (int it = 0; it < stab; ++it) {
+      if ((rc = sweep(S, it, st)) != GG_OK) return rc;
+      if ((rc = apply(S, it, true, false, st)) != GG_OK) return rc;
+    }
+    const int cap = std::max(0, std::min(S->P.max_sweeps, kMaxSweeps - stab));
+    int k = 0;
+    float res = 0.0f;
+    for (;;) {
+      if ((rc = residual(S, st, &res)) != GG_OK) return rc;
+      if (!(res > S->P.target_residual) || k >= cap) break;
+      if ((rc = sweep(S, stab + k, st)) != GG_OK) return rc;
+      if ((rc = apply(S, stab + k, false, true, st)) != GG_OK) return rc;
+      ++k;
+    }
+    S->last_sweeps = k;
+    S->last_residual = res;
+  } else {
+    const int total = std::min(S->P.stab_iters + S->P.iters, kMaxSweeps);
+    for (int it = 0; it < total; ++it) {
+      if ((rc = sweep(S, it, st)) != GG_OK) return rc;
+      if ((rc = apply(S, it, it < S->P.stab_iters, it == total - 1, st)) != GG_OK) return rc;
+    }
   }
+  if (S->P.warm_start == 2 && (rc = warm_start_target(S, st)) != GG_OK) return rc;
   if ((rc = finalize(S, st)) != GG_OK) return rc;
   if (S->P.upsample_enabled && (rc = upsample(S, st)) != GG_OK) return rc;
   if (S->phys.is_adaptive == 1 && S->P.merge_enabled && S->n > 0) {
@@ -185,7 +211,7 @@ static void free_all(gg_system* S) {
                   G.ncon, G.keys, G.perm, G.cell_start, G.prop, G.ldens, G.winner, G.split_flag, G.keep_flag,
                   G.split_slot, G.keep_slot, G.child_pos, G.nl_idx, G.nl_meta, G.nl_acc, G.nl_queue, G.cell_inc, S->b.pos, S->b.animated, S->b.pos_alt,
                   S->b.animated_alt, S->b.keys, S->b.perm, S->b.cell_start, S->u.keys, S->u.perm, S->scal,
-                  S->stats_partial, S->stage};
+                  S->stats_partial, S->stage, S->feat, S->xs0, S->warm_target};
   for (void* p : ptrs) cudaFree(p);
   if (S->scal_host) cudaFreeHost(S->scal_host);
   sort_scratch_free(S->sort);
@@ -497,6 +523,9 @@ gg_status stats_compute(gg_system* S, gg_stats_t* out) {
   memcpy(&pen, &pen_bits, sizeof(pen));
   out->max_penetration = pen;
   out->error_word = S->error_word;
+  out->last_sweeps = S->last_sweeps;
+  out->last_residual = S->last_residual;
+  out->last_residual_max = S->last_residual_max;
   return GG_OK;
 }
 

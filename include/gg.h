@@ -72,7 +72,10 @@ typedef enum gg_field {
   GG_FIELD_ADAPTIVE_LAST_STEP = 13, /* int32   get_adaptive_last_step_ptr (granular) */
   GG_FIELD_IS_ANIMATED = 14,      /* int32     get_is_animated_ptr (boundary) */
   GG_FIELD_CONTACTS = 15,         /* int32     contacts found by each particle in the last sweep (granular) */
-  GG_FIELD_NUM_CONSTRAINTS = 16   /* int32     constraint count n_i of the last sweep (granular) */
+  GG_FIELD_NUM_CONSTRAINTS = 16,  /* int32     constraint count n_i of the last sweep (granular) */
+  GG_FIELD_FEATURES = 17,         /* uint16[48] bf16 warm-start features of the last substep (granular) */
+  GG_FIELD_WARM_TARGET = 18       /* float[3]  correction the sweeps reached, x*_final - x*_predict, in
+                                     units of |g| dt^2 (granular, warm_start = 2) */
 } gg_field;
 
 /*
@@ -125,7 +128,21 @@ typedef struct gg_params {
                                   cell length; 0 = scan the stencil every sweep.  Results do
                                   not depend on it, only the speed and memory (148 bytes per
                                   particle of capacity) do. */
-  int32_t reserved[6];
+  float target_residual;       /* > 0: after the stabilisation sweeps, Jacobi sweeps run until the
+                                  mean penetration over the contacts at x* (particle pairs
+                                  r_i + r_j - |x_i - x_j| > 0 and walls), measured before each sweep,
+                                  is at most this length, or max_sweeps sweeps have run; `iters` is
+                                  then unused.  0 (default): the fixed `iters` sweeps of the
+                                  reference.  No counterpart in the reference. */
+  int32_t max_sweeps;          /* cap on the Jacobi sweeps of a substep in residual mode (default 200;
+                                  stab_iters + max_sweeps is capped at 256) */
+  int32_t warm_start;          /* 0 (default) off; 1 = before the sweeps, add the attached network's
+                                  predicted correction to x* (gg_set_warm_start); 2 = record the
+                                  features and, after the sweeps, the correction the sweeps reached
+                                  (GG_FIELD_FEATURES, GG_FIELD_WARM_TARGET: training data).  No
+                                  counterpart in the reference. */
+  float warm_start_scale;      /* multiplies the predicted correction (default 1) */
+  int32_t reserved[2];         /* testing switches: [0] sweep kernel variant, [1] stencil-kernel variant */
 } gg_params;
 
 /* Arguments of GranularSystem::GranularSystem, GranularSystem.hpp:8-14. */
@@ -181,6 +198,10 @@ typedef struct gg_stats_t {
   int32_t nonfinite;           /* particles with a NaN/Inf position */
   int32_t error_word;          /* device error bits (capacity, timeout) since create */
   int64_t launches;            /* kernels this library launched since create */
+  int32_t last_sweeps;         /* Jacobi sweeps of the last substep in residual mode */
+  float last_residual;         /* mean penetration over contacts at the last check (residual mode) */
+  float last_residual_max;     /* largest penetration at the last check (residual mode) */
+  int32_t pad_;
 } gg_stats_t;
 
 /* Per-kernel-class timing accumulated between gg_profile_begin/_end. */
@@ -219,6 +240,14 @@ gg_status gg_scene_build(const char* json_path, const char* base_dir,
                          float* boundary, int32_t* boundary_animated, int64_t* n_boundary,
                          float* upsampled, int64_t* n_upsampled,
                          gg_desc* desc_out);
+
+/* The parameters in use, and a change of them between substeps (for example
+ * switching the warm start or the residual mode).  nlist_skin cannot change
+ * after gg_create (it sizes the contact lists): a different value returns
+ * GG_ERR_NOT_SUPPORTED.  No counterpart in the reference (its constants are
+ * compiled in). */
+gg_status gg_get_params(gg_system* sys, gg_params* out);
+gg_status gg_set_params(gg_system* sys, const gg_params* params);
 
 /* GranularSystem::step (GranularSystem.cu:397-453), n_substeps times.
  * Asynchronous on the system's stream. */
@@ -347,6 +376,11 @@ gg_status gg_mlp_gradient(gg_mlp* mlp, const void* d_features, const float* d_ta
 gg_status gg_mlp_train_step(gg_mlp* mlp, const void* d_features, const float* d_targets, int64_t n, float lr,
                             float weight_decay, float* host_loss, void* stream);
 void gg_mlp_destroy(gg_mlp* mlp);
+/* Attaches a network to a system for gg_params.warm_start = 1 (mlp may be
+ * NULL for warm_start = 2) and allocates the warm-start buffers (feature,
+ * predicted-position and target arrays: 124 bytes per particle of
+ * capacity).  The network must outlive its use by the system. */
+gg_status gg_set_warm_start(gg_system* sys, gg_mlp* mlp);
 
 #ifdef __cplusplus
 }
