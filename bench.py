@@ -303,6 +303,12 @@ def run_mine(args):
         "gpu_launches": int(launches),
         "clocks": clocks,
     }
+    if rank == 0 and world == 1 and not args.no_batched:
+        # batched scenes: 64 scenes in one system, autotuned, replayed as a
+        # CUDA graph, against the same scenes stepped one after another
+        from granular_gpu_gb300 import batch
+        line["batched_scenes"] = batch.measure(64, frames=args.batched_frames, device=local)
+        line["batched_scenes"]["unit"] = METRIC
     if rank == 0 and world == 1 and not args.no_learned:
         # learned warm start vs the plain sweeps, to the same residual, on a
         # held-out scene (device time of whole substeps, CUDA events)
@@ -344,6 +350,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-learned", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--batched-frames", type=int, default=10)
     ap.add_argument("--learned-frames", type=int, default=150)
     ap.add_argument("--counts", default="128,256,256",
                     help="column lattice x,y,z (the benchmark workload is 128,256,256)")

@@ -149,6 +149,12 @@ class gg_stats_t(C.Structure):
     ]
 
 
+class gg_tuning(C.Structure):
+    _fields_ = [("predict_threads", C.c_int32), ("apply_threads", C.c_int32), ("finalize_threads", C.c_int32),
+                ("keep_threads", C.c_int32), ("build_blocks_per_sm", C.c_int32), ("trials", C.c_int32),
+                ("ms_default", C.c_float), ("ms_tuned", C.c_float)]
+
+
 GG_PROF_MAX = 24
 
 
@@ -213,6 +219,11 @@ SIGNATURES = {
     "gg_mlp_destroy": (None, [P_]),
     "gg_set_warm_start": (C.c_int, [P_, P_]),
     "gg_get_params": (C.c_int, [P_, C.POINTER(gg_params)]),
+    "gg_set_scenes": (C.c_int, [P_, C.c_int32, C.c_float, C.POINTER(C.c_float)]),
+    "gg_scene_stats": (C.c_int, [P_, C.POINTER(C.c_double), C.c_int32]),
+    "gg_graph_capture": (C.c_int, [P_, C.c_int32]),
+    "gg_graph_launch": (C.c_int, [P_]),
+    "gg_autotune": (C.c_int, [P_, C.c_int32, C.POINTER(gg_tuning)]),
     "gg_set_params": (C.c_int, [P_, C.POINTER(gg_params)]),
 }
 

@@ -766,3 +766,116 @@ void gg_grid_destroy(gg_grid* g) {
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------ autotuning
+
+gg_status gg_autotune(gg_system* S, int32_t substeps, gg_tuning* out) {
+  GG_GUARD_BEGIN
+  REQUIRE(S && substeps > 0, "gg_autotune: bad argument");
+  REQUIRE(!S->graph_exec, "gg_autotune: tune before capturing a graph (the graph keeps its launch shapes)");
+  REQUIRE(!((S->phys.is_adaptive == 1 && S->P.merge_enabled) || S->P.target_residual > 0.0f),
+          "gg_autotune: needs a fixed-length substep (no merge/split, no residual mode)");
+  GG_CUDA(cudaSetDevice(S->device));
+  cudaStream_t st = S->stream;
+  GG_CUDA(cudaStreamSynchronize(st));
+  // device copy of the state; every trial starts from it
+  const std::vector<Blob> blobs = snapshot_blobs(S);
+  size_t total = 0;
+  for (const Blob& b : blobs) total += (b.bytes + 255) & ~(size_t)255;
+  char* backup = nullptr;
+  GG_CUDA(cudaMalloc((void**)&backup, std::max<size_t>(total, 1)));
+  auto copy_all = [&](bool save) -> cudaError_t {
+    size_t off = 0;
+    for (const Blob& b : blobs) {
+      cudaError_t e = b.bytes ? cudaMemcpyAsync(save ? backup + off : b.dptr, save ? b.dptr : backup + off, b.bytes,
+                                                cudaMemcpyDeviceToDevice, st)
+                              : cudaSuccess;
+      if (e != cudaSuccess) return e;
+      off += (b.bytes + 255) & ~(size_t)255;
+    }
+    return cudaStreamSynchronize(st);
+  };
+  const int cur0 = S->g.cur, ucur0 = S->u.cur;
+  const int64_t steps0 = S->steps, launches0 = S->launches, n_grid0 = S->n_grid;
+  const bool timing0 = S->frame_timing;
+  S->frame_timing = false;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaError_t ce = copy_all(true);
+  if (ce == cudaSuccess) ce = cudaEventCreate(&e0);
+  if (ce == cudaSuccess) ce = cudaEventCreate(&e1);
+  gg_status rc = ce == cudaSuccess ? GG_OK : cuda_status(ce, "gg_autotune: state copy");
+  int trials = 0;
+  // device ms of `substeps` substeps after one warm-up substep, from the saved state
+  auto trial = [&](float* ms) -> gg_status {
+    cudaError_t e = copy_all(false);
+    if (e != cudaSuccess) return cuda_status(e, "gg_autotune: restore");
+    S->g.cur = cur0;
+    S->u.cur = ucur0;
+    S->n_grid = n_grid0;
+    gg_status r = step_once(S);
+    if (r != GG_OK) return r;
+    GG_CUDA(cudaEventRecord(e0, st));
+    for (int k = 0; k < substeps && r == GG_OK; ++k) r = step_once(S);
+    if (r != GG_OK) return r;
+    GG_CUDA(cudaEventRecord(e1, st));
+    GG_CUDA(cudaEventSynchronize(e1));
+    GG_CUDA(cudaEventElapsedTime(ms, e0, e1));
+    ++trials;
+    return GG_OK;
+  };
+  float base = 0.0f, best = 0.0f;
+  if (rc == GG_OK) rc = trial(&base);
+  best = base;
+  struct Site {
+    int* field;
+    std::vector<int> cands;
+  };
+  Tuning& T = S->tune;
+  std::vector<Site> sites = {{&T.keep_threads, {128, 256}},
+                             {&T.build_blocks_per_sm, {4, 8, 16, 32}},
+                             {&T.apply_threads, {128, 256}},
+                             {&T.predict_threads, {128, 256}},
+                             {&T.finalize_threads, {64, 128, 256}}};
+  for (Site& site : sites) {
+    if (rc != GG_OK) break;
+    const int keep = *site.field;
+    int choice = keep;
+    for (int c : site.cands) {
+      if (c == keep) continue;
+      *site.field = c;
+      float ms = 0.0f;
+      rc = trial(&ms);
+      if (rc != GG_OK) break;
+      if (ms < best) {
+        best = ms;
+        choice = c;
+      }
+    }
+    *site.field = choice;
+  }
+  // leave the system as it was, with the chosen shapes
+  cudaError_t re = copy_all(false);
+  S->g.cur = cur0;
+  S->u.cur = ucur0;
+  S->n_grid = n_grid0;
+  S->steps = steps0;
+  S->launches = launches0;
+  S->frame_timing = timing0;
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaFree(backup);
+  if (rc != GG_OK) return rc;
+  GG_CUDA(re);
+  if (out) {
+    out->predict_threads = T.predict_threads;
+    out->apply_threads = T.apply_threads;
+    out->finalize_threads = T.finalize_threads;
+    out->keep_threads = T.keep_threads;
+    out->build_blocks_per_sm = T.build_blocks_per_sm;
+    out->trials = trials;
+    out->ms_default = base;
+    out->ms_tuned = best;
+  }
+  return GG_OK;
+  GG_GUARD_END
+}

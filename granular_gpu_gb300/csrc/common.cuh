@@ -146,6 +146,21 @@ __device__ __forceinline__ void block_max_bits(unsigned int* dst, unsigned int v
   __syncthreads();  // s_max is reused by the next call
 }
 
+// The same for any block of at most 256 threads (a multiple of 32), the
+// size read at run time, so that the launch shape can be tuned.
+__device__ __forceinline__ void block_max_bits_any(unsigned int* dst, unsigned int v) {
+  __shared__ unsigned int s_max[8];
+  v = __reduce_max_sync(0xffffffffu, v);
+  if ((threadIdx.x & 31) == 0) s_max[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    unsigned int m = threadIdx.x < (blockDim.x >> 5) ? s_max[threadIdx.x] : 0u;
+    m = __reduce_max_sync(0xffffffffu, m);
+    if (threadIdx.x == 0 && m) atomicMax(dst, m);
+  }
+  __syncthreads();  // s_max is reused by the next call
+}
+
 __device__ __forceinline__ unsigned int lanemask_lt() {
   unsigned int m;
   asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));

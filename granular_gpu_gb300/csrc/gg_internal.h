@@ -139,6 +139,16 @@ struct Physics {
 
 }  // namespace gg
 
+// Launch shapes chosen by gg_autotune (defaults: the shapes written in the
+// kernels' launch bounds).
+struct Tuning {
+  int predict_threads = 256;
+  int apply_threads = 256;
+  int finalize_threads = 256;
+  int keep_threads = 256;
+  int build_blocks_per_sm = 16;
+};
+
 struct gg_system {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -161,6 +171,16 @@ struct gg_system {
   void* feat = nullptr;                // cap x 48 bf16 features of the last substep
   float4* xs0 = nullptr;               // cap: x* after the predict (warm_start = 2)
   float* warm_target = nullptr;        // cap x 3: (x*_final - x*_predict) / (|g| dt^2)
+  // batched scenes (gg_set_scenes): scene k is the slab k*width <= x < (k+1)*width
+  int n_scenes = 0;
+  float scene_width = 0.0f;
+  float* scene_fcap = nullptr;         // device, per scene
+  double* scene_acc = nullptr;         // device, per scene x kSceneStats
+  // a captured substep sequence (gg_graph_capture)
+  cudaGraphExec_t graph_exec = nullptr;
+  int graph_substeps = 0;
+  int64_t graph_launches = 0;          // kernels per graph launch
+  Tuning tune;
   int32_t last_sweeps = 0;
   float last_residual = 0.0f;         // mean penetration over contacts
   float last_residual_max = 0.0f;     // largest penetration

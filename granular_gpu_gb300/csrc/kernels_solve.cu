@@ -57,8 +57,8 @@ __global__ void k_predict(int n, const float4* __restrict__ pos, const float4* _
     rbits = __float_as_uint(fabsf(p.w));
     dbits = __float_as_uint(fmaxf(fmaxf(fabsf(x.x - p.x), fabsf(x.y - p.y)), fabsf(x.z - p.z)));
   }
-  block_max_bits<256>(&scal->rmax_bits, rbits);
-  block_max_bits<256>(&scal->disp0_bits, dbits);
+  block_max_bits_any(&scal->rmax_bits, rbits);
+  block_max_bits_any(&scal->disp0_bits, dbits);
 }
 
 gg_status predict(gg_system* S, cudaStream_t st) {
@@ -68,7 +68,8 @@ gg_status predict(gg_system* S, cudaStream_t st) {
   const float3 dv = make_float3(dt * S->phys.g.x, dt * S->phys.g.y, dt * S->phys.g.z);
   prof_begin(S, PC_PREDICT, st);
   auto kern = S->P.math_mode ? k_predict<1> : k_predict<0>;
-  kern<<<blocks_for(S->n, 256), 256, 0, st>>>((int)S->n, S->g.pos[c], S->g.vel[c], S->g.mass[c], S->g.xs,
+  const int tp = S->tune.predict_threads;
+  kern<<<blocks_for(S->n, tp), tp, 0, st>>>((int)S->n, S->g.pos[c], S->g.vel[c], S->g.mass[c], S->g.xs,
                                                    S->g.inv_m, dt, dv, S->scal);
   count_launches(S, 1);
   prof_end(S, PC_PREDICT, S->n, st);
@@ -124,7 +125,7 @@ __global__ void __launch_bounds__(256) k_apply(int n, float4* __restrict__ xs, f
     const unsigned m = __reduce_max_sync(peers, bits);
     if (key != 0xffffffffu && m && (threadIdx.x & 31) == __ffs(peers) - 1) atomicMax(&cell_inc[key], m);
   }
-  block_max_bits<256>(inc_bits, bits);
+  block_max_bits_any(inc_bits, bits);
 }
 
 gg_status apply(gg_system* S, int it, bool stab, bool last, cudaStream_t st) {
@@ -133,7 +134,8 @@ gg_status apply(gg_system* S, int it, bool stab, bool last, cudaStream_t st) {
   // the listed sweep after this one reads the per-cell increments
   uint32_t* cell_inc = (S->g.cell_inc && !last) ? S->g.cell_inc : nullptr;
   if (cell_inc) GG_CUDA(cudaMemsetAsync(cell_inc, 0, sizeof(uint32_t) * ((size_t)S->grid.C + 1), st));
-  k_apply<<<blocks_for(S->n, 256), 256, 0, st>>>((int)S->n, S->g.xs, S->g.pos[S->g.cur], S->g.delta,
+  const int ta = S->tune.apply_threads;
+  k_apply<<<blocks_for(S->n, ta), ta, 0, st>>>((int)S->n, S->g.xs, S->g.pos[S->g.cur], S->g.delta,
                                                  S->g.s_extra, S->g.ncon, S->g.contacts, stab ? 1 : 0,
                                                  last ? 1 : 0, &S->scal->inc_bits[it], S->g.keys, cell_inc);
   count_launches(S, 1);
@@ -188,7 +190,8 @@ gg_status finalize(gg_system* S, cudaStream_t st) {
   const int c = S->g.cur;
   prof_begin(S, PC_FINALIZE, st);
   auto kern = S->P.math_mode ? k_finalize<1> : k_finalize<0>;
-  kern<<<blocks_for(S->n, 256), 256, 0, st>>>((int)S->n, S->g.pos[c], S->g.xs, S->g.vel[c], S->g.als[c], f);
+  const int tf = S->tune.finalize_threads;
+  kern<<<blocks_for(S->n, tf), tf, 0, st>>>((int)S->n, S->g.pos[c], S->g.xs, S->g.vel[c], S->g.als[c], f);
   count_launches(S, 1);
   prof_end(S, PC_FINALIZE, S->n, st);
   GG_CUDA(cudaGetLastError());

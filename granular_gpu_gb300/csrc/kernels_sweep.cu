@@ -57,6 +57,11 @@ struct SweepArgs {
   int cap;
   float skin;
   float eabs;    // bound on the rounding of one position update
+  // batched scenes: scene of a particle = its x* slab, floor(x / width);
+  // each scene has its own friction cap (null: a.fcap for every particle)
+  const float* __restrict__ scene_fcap;
+  float scene_inv_w;
+  int n_scenes;
 };
 
 // Which of the three cell columns [c-1, c, c+1] along one axis can hold a
@@ -87,6 +92,7 @@ struct Target {
   bool binned;
   int cx, cy, cz; // binning cell
   unsigned pm[3], bm[3];
+  double fcap;    // friction cap factor (0.8 in the reference; per scene in a batch)
 };
 
 // The per-target values every sweep needs (no pruning masks).
@@ -97,7 +103,12 @@ __device__ __forceinline__ void make_target_lite(const SweepArgs& a, int i, floa
   t.rb = fmaxf(t.rc, a.minr);
   t.Bd = a.brad + (double)t.rb;
   t.Bru = __double2float_ru(t.Bd);
-  t.capBru = __double2float_ru(((double)t.rb + a.brad) * a.fcap);
+  t.fcap = a.fcap;
+  if (a.scene_fcap) {
+    const int s = min(max(__float2int_rz(t.x.x * a.scene_inv_w), 0), a.n_scenes - 1);
+    t.fcap = (double)a.scene_fcap[s];
+  }
+  t.capBru = __double2float_ru(((double)t.rb + a.brad) * t.fcap);
   const float Bf = (float)t.Bd;
   t.Bcut = Bf * Bf * 1.0001f;
   t.inv_m = a.inv_m[i];
@@ -155,7 +166,7 @@ __device__ __forceinline__ void wall_contact(const SweepArgs& a, const Target& t
   if (pn < t.capBru) {
     dp = sub3(dp, dpi);
   } else {
-    const float minf = (float)fmin((a.brad + (double)t.rb) * a.fcap / (double)pn, 1.0);
+    const float minf = (float)fmin((a.brad + (double)t.rb) * t.fcap / (double)pn, 1.0);
     dp = sub3(dp, mul3s(dpi, minf));
   }
   ++c;
@@ -198,7 +209,7 @@ __device__ __forceinline__ void particle_pair_f(const SweepArgs& a, const Target
   const float3 dpj = smul3((inv_sum * inv_mj) * tt, p12);
   const float3 dpij = sub3(dpi, dpj);
   const float w = inv_sum * t.inv_m;
-  const float capf = rr * (float)a.fcap;
+  const float capf = rr * (float)t.fcap;
   // The tangential part `perp` of dpij (which is parallel to p12) is
   // rounding noise: |perp| <= 2 (|a| + |b|) dis (1 + 8 eps) with a, b the
   // two scalar factors above.  When that bound is below the cap the
@@ -214,12 +225,12 @@ __device__ __forceinline__ void particle_pair_f(const SweepArgs& a, const Target
     // (double)pn < (double)rr * 0.8, decided in float when clear-cut
     if (pn < capf * 0.999999f) within = true;
     else if (pn > capf * 1.000001f) within = false;
-    else within = (double)pn < (double)rr * a.fcap;
+    else within = (double)pn < (double)rr * t.fcap;
   }
   if (within) {
     dp = sub3(dp, smul3(w, dpij));
   } else {
-    const float minf = (float)fmin((double)rr * a.fcap / (double)pn, 1.0);
+    const float minf = (float)fmin((double)rr * t.fcap / (double)pn, 1.0);
     dp = sub3(dp, mul3s(smul3(w, dpij), minf));
   }
   ++c;
@@ -922,6 +933,9 @@ gg_status sweep(gg_system* S, int it, cudaStream_t st) {
   a.scal = S->scal;
   a.brad = S->P.boundary_radius;
   a.fcap = S->P.friction_cap;
+  a.scene_fcap = S->scene_fcap;
+  a.scene_inv_w = S->scene_width > 0.0f ? 1.0f / S->scene_width : 0.0f;
+  a.n_scenes = S->n_scenes;
   a.minr = S->P.boundary_min_radius;
   a.nl_idx = S->g.nl_idx;
   a.nl_meta = S->g.nl_meta;
@@ -966,8 +980,9 @@ gg_status sweep(gg_system* S, int it, cudaStream_t st) {
         build<<<blocks_for(S->n, kBuildThreads), kBuildThreads, 0, st>>>(a, 0);
       } else {
         auto keep = S->P.math_mode ? k_sweep_nlist_keep<1> : k_sweep_nlist_keep<0>;
-        keep<<<blocks_for(S->n, 256), 256, 0, st>>>(a);
-        const int nb = std::min(blocks_for(S->n, kBuildThreads), S->num_sms * 16);
+        const int tk = S->tune.keep_threads;
+        keep<<<blocks_for(S->n, tk), tk, 0, st>>>(a);
+        const int nb = std::min(blocks_for(S->n, kBuildThreads), S->num_sms * S->tune.build_blocks_per_sm);
         build<<<nb, kBuildThreads, 0, st>>>(a, 1);
         count_launches(S, 1);
       }

@@ -211,7 +211,8 @@ static void free_all(gg_system* S) {
                   G.ncon, G.keys, G.perm, G.cell_start, G.prop, G.ldens, G.winner, G.split_flag, G.keep_flag,
                   G.split_slot, G.keep_slot, G.child_pos, G.nl_idx, G.nl_meta, G.nl_acc, G.nl_queue, G.cell_inc, S->b.pos, S->b.animated, S->b.pos_alt,
                   S->b.animated_alt, S->b.keys, S->b.perm, S->b.cell_start, S->u.keys, S->u.perm, S->scal,
-                  S->stats_partial, S->stage, S->feat, S->xs0, S->warm_target};
+                  S->stats_partial, S->stage, S->feat, S->xs0, S->warm_target, S->scene_fcap,
+                  S->scene_acc};
   for (void* p : ptrs) cudaFree(p);
   if (S->scal_host) cudaFreeHost(S->scal_host);
   sort_scratch_free(S->sort);
@@ -418,6 +419,7 @@ void system_destroy(gg_system* S) {
   if (!S) return;
   cudaSetDevice(S->device);
   cudaStreamSynchronize(S->stream);
+  if (S->graph_exec) cudaGraphExecDestroy(S->graph_exec);
   free_all(S);
   delete S;
 }

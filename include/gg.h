@@ -352,6 +352,45 @@ gg_status gg_grid_build_noalloc(int32_t device, const float* d_pos, int64_t n,
                                 int32_t* d_cell_start, void* stream);
 
 /*
+ * Batched scenes.  No counterpart in the reference (one scene per
+ * GranularSystem there).  A batch is one system whose particles and walls
+ * hold many independent scenes side by side along x: scene k occupies the
+ * slab k*width <= x < (k+1)*width, its box walls inside the slab, with at
+ * least one empty cell between neighbouring boxes so that no contact
+ * crosses scenes.  One grid, one sort and one launch of each kernel then
+ * step every scene.
+ */
+/* Declares the slabs; friction_cap (optional, n_scenes values) replaces
+ * gg_params.friction_cap per scene. */
+gg_status gg_set_scenes(gg_system* sys, int32_t n_scenes, float width, const float* friction_cap);
+/* FP64 per-scene diagnostics, 9 doubles per scene: particle count, mass,
+ * momentum x y z, kinetic energy, centre of mass x y z. */
+gg_status gg_scene_stats(gg_system* sys, double* host_out, int32_t n_scenes);
+/* Captures n_substeps substeps (an even number: the graph replays fixed
+ * addresses of the double-buffered arrays) into a CUDA graph on the
+ * system's stream (no merge/split, residual mode, moving walls, profiling
+ * or frame timing), to be replayed by gg_graph_launch, asynchronously, as
+ * often as wanted. */
+gg_status gg_graph_capture(gg_system* sys, int32_t n_substeps);
+gg_status gg_graph_launch(gg_system* sys);
+
+/* Launch shapes chosen by gg_autotune. */
+typedef struct gg_tuning {
+  int32_t predict_threads, apply_threads, finalize_threads; /* threads per block */
+  int32_t keep_threads;        /* threads per block of the contact-list sweep */
+  int32_t build_blocks_per_sm; /* resident blocks per SM of the list-rebuild sweep */
+  int32_t trials;              /* timed trials run */
+  float ms_default, ms_tuned;  /* device ms of `substeps` substeps with the shapes before and after */
+} gg_tuning;
+/* Times `substeps` substeps for each candidate launch shape of the
+ * substep's tunable kernels, one kernel at a time, every trial from the same
+ * saved state (restored afterwards: the system is left as it was), and
+ * keeps the fastest shapes.  Needs a fixed-length substep (no merge/split,
+ * no residual mode); call before gg_graph_capture.  Allocates a device copy
+ * of the state while it runs. */
+gg_status gg_autotune(gg_system* sys, int32_t substeps, gg_tuning* out);
+
+/*
  * Learned warm start.  No counterpart in the reference: a 48 -> 64 -> 64 -> 3
  * MLP (ReLU, BF16 weights on the tensor cores, FP32 accumulation) that
  * predicts a substep's Jacobi position correction from per-particle
