@@ -56,6 +56,23 @@ __device__ __forceinline__ void for_each_stencil_column(const Grid& g, int3 q, F
   }
 }
 
+// The same walk that stops as soon as f returns true.
+template <class F>
+__device__ __forceinline__ void for_each_stencil_column_until(const Grid& g, int3 q, F&& f) {
+  const long long zl = max((long long)q.z - 1, 0LL);
+  const long long zh = min((long long)q.z + 1, (long long)g.nz - 1);
+  if (zl > zh) return;
+  for (int ox = -1; ox <= 1; ++ox) {
+    const long long x = (long long)q.x + ox;
+    if (x < 0 || x >= g.nx) continue;
+    for (int oy = -1; oy <= 1; ++oy) {
+      const long long y = (long long)q.y + oy;
+      if (y < 0 || y >= g.ny) continue;
+      if (f((int)((x * g.ny + y) * g.nz + zl), (int)(zh - zl + 1))) return;
+    }
+  }
+}
+
 // sqrtf(dd) > X, with the clear cases decided from dd against X*X: beyond
 // a relative margin of 2e-6 on the square the rounded root lies several
 // ulps from X.  Near-ties, and X*X outside the normal range, take the root.

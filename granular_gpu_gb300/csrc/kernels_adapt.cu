@@ -17,6 +17,12 @@ namespace gg {
 
 // find_cover_vector + find_surface (GranularSystem.cu:506-611) fused: the
 // cover vector of i is only needed by i, so one thread makes both passes.
+// The second pass of the reference counts the neighbours within
+// 2 (r_i + r_j) (the same set the first pass sums over, with the same
+// distance test) and ORs a cone vote over them; the flag only depends on
+// (count <= 5 || !vote).  So the count comes from the first pass, a count
+// of at most 5 decides the flag without a second pass, and the second pass
+// stops at the first vote: the flags are the reference's.
 template <int MM>
 __global__ void __launch_bounds__(256) k_surface(Grid g, int n, const float4* __restrict__ pos,
                                                  const float* __restrict__ rs, const int32_t* __restrict__ cs,
@@ -27,6 +33,7 @@ __global__ void __launch_bounds__(256) k_surface(Grid g, int n, const float4* __
   const float ri = rs[i];
   const int3 q = trunc_cell(g, xi);
   float3 cv = make_float3(0.f, 0.f, 0.f);
+  unsigned nn = 0;
   for_each_stencil_column(g, q, [&](int k0, int nc) {
     const int j1 = cs[k0 + nc];
     for (int j = cs[k0]; j < j1; ++j) {
@@ -34,26 +41,30 @@ __global__ void __launch_bounds__(256) k_surface(Grid g, int n, const float4* __
       const float3 d = sub3(xi, f3(pos[j]));
       if (sqrt_gt(dot3(d, d), 2.0f * (ri + rs[j]))) continue;
       cv = add3(cv, m_normalize3<MM>(d));
+      ++nn;
     }
   });
+  if (nn <= (unsigned)min_nb) {
+    surface[i] = 1;
+    return;
+  }
   const float3 c = m_normalize3<MM>(cv);
   bool vote = false;
-  unsigned nn = 0;
-  for_each_stencil_column(g, q, [&](int k0, int nc) {
+  for_each_stencil_column_until(g, q, [&](int k0, int nc) {
     const int j1 = cs[k0 + nc];
     for (int j = cs[k0]; j < j1; ++j) {
       if (j == i) continue;
       float3 b = sub3(f3(pos[j]), xi);
       if (sqrt_gt(dot3(b, b), 2.0f * (ri + rs[j]))) continue;
-      // the vote is an OR: once set, later angles cannot change it
-      if (!vote) {
-        b = m_normalize3<MM>(b);
-        if (m_acos<MM>(dot3(b, c)) <= cone) vote = true;
+      b = m_normalize3<MM>(b);
+      if (m_acos<MM>(dot3(b, c)) <= cone) {
+        vote = true;
+        return true;
       }
-      ++nn;
     }
+    return false;
   });
-  surface[i] = (nn <= (unsigned)min_nb || !vote) ? 1 : 0;
+  surface[i] = vote ? 0 : 1;
 }
 
 // Warp-cooperative form of k_surface (same sums, same order).

@@ -315,13 +315,18 @@ __global__ void __launch_bounds__(kTile, 1) k_mlp_fwd(const __grid_constant__ CU
   const uint32_t aX = tc::smem_u32(sX), aH = tc::smem_u32(sH), aW = tc::smem_u32(sW);
   const int ntiles = (a.n + kTile - 1) / kTile;
   unsigned int dmax = 0;
-  for (int tile = blockIdx.x; ok && tile < ntiles; tile += gridDim.x) {
-    if (t == 0) {
-      tc::mbar_arrive_expect_tx(&bars[1], kTile * kFeat * 2);
+  // The X tile is loaded by TMA one tile ahead: as soon as layer 1 has read
+  // it, the next tile's copy is issued and overlaps layers 2 and 3.
+  auto load_x = [&](int tile) {
+    tc::mbar_arrive_expect_tx(&bars[1], kTile * kFeat * 2);
 #pragma unroll
-      for (int c = 0; c < kFeat / 8; ++c) tc::tensor_g2s_2d(sX + c * kTile * 16, &tmX, 8 * c, tile * kTile, &bars[1]);
-    }
+    for (int c = 0; c < kFeat / 8; ++c) tc::tensor_g2s_2d(sX + c * kTile * 16, &tmX, 8 * c, tile * kTile, &bars[1]);
+  };
+  bool x_pending = ok && (int)blockIdx.x < ntiles;  // a tile copy is in flight (same in every thread)
+  if (t == 0 && x_pending) load_x(blockIdx.x);
+  for (int tile = blockIdx.x; ok && tile < ntiles; tile += gridDim.x) {
     if (!(ok = wait_all(&bars[1], ph_x, a.err, failed))) break;
+    x_pending = false;
     // layer 1: D[0, 64) = X W1
     if (t == 0) {
       tc::fence_after_sync();
@@ -332,6 +337,10 @@ __global__ void __launch_bounds__(kTile, 1) k_mlp_fwd(const __grid_constant__ CU
       tc::mma_commit(&bars[2]);
     }
     if (!(ok = wait_all(&bars[2], ph_m, a.err, failed))) break;
+    if (tile + (int)gridDim.x < ntiles) {
+      x_pending = true;
+      if (t == 0) load_x(tile + gridDim.x);
+    }
     tc::fence_after_sync();
     const int r = warp * 32 + lane;
 #pragma unroll
@@ -398,6 +407,7 @@ __global__ void __launch_bounds__(kTile, 1) k_mlp_fwd(const __grid_constant__ CU
     __syncthreads();
   }
   drain(failed);
+  if (x_pending && failed.bar != &bars[1]) tc::mbar_wait(&bars[1], ph_x, kWaitPolls);
   if (kApply) warp_max_bits(a.disp_bits, dmax);
   tc::fence_before_sync();
   __syncthreads();
@@ -801,7 +811,8 @@ gg_status mlp_forward(gg_mlp* M, const void* X, int64_t n, float* y, float4* xs,
   a.disp_bits = disp_bits;
   a.err = M->err;
   const int ntiles = (int)((n + kTile - 1) / kTile);
-  const int grid = std::max(1, std::min(ntiles, 2 * M->num_sms));
+  // four CTAs per SM (57 KB of shared memory and 128 TMEM columns each)
+  const int grid = std::max(1, std::min(ntiles, 4 * M->num_sms));
   if (xs) {
     GG_CUDA(cudaFuncSetAttribute(k_mlp_fwd<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kFwSmem));
     k_mlp_fwd<true><<<grid, kTile, kFwSmem, st>>>(map, a);
