@@ -184,7 +184,10 @@ def main(argv=None):
     import json
     import time
     ap = argparse.ArgumentParser(description="train or evaluate the learned warm start")
-    ap.add_argument("cmd", choices=["train", "evaluate"])
+    ap.add_argument("cmd", choices=["train", "evaluate", "bench"],
+                    help="train: collect and train; evaluate: plain vs warm start; "
+                         "bench: time the network's kernels on random features")
+    ap.add_argument("--rows", type=int, default=1 << 22, help="feature rows (bench)")
     ap.add_argument("--scenes", type=int, default=8)
     ap.add_argument("--frames", type=int, default=250, help="frames per training scene (train) or per run (evaluate)")
     ap.add_argument("--per-frame", type=int, default=4096)
@@ -212,11 +215,49 @@ def main(argv=None):
                           "collect_s": round(t1 - t0, 2), "train_s": round(t2 - t1, 2),
                           "loss_first": losses[0], "loss_last": float(np.mean(losses[-100:])),
                           "target_variance": float(T.var().item()), "weights": a.weights}))
-    else:
+    elif a.cmd == "evaluate":
         m = load_mlp(a.weights)
         seeds = tuple(int(s) for s in a.eval_seeds.split(","))
         print(json.dumps(evaluate(m, seeds=seeds, frames=a.frames, tol=a.tol)))
+    else:
+        print(json.dumps(bench_kernels(a.rows, seed=a.seed)))
     return 0
+
+
+def bench_kernels(n: int, seed: int = 0, reps: int = 10) -> dict:
+    """Device time of the network's forward and gradient kernels over n
+    random bf16 feature rows (three untimed forward + training passes
+    first), with the work they issue to the tensor cores."""
+    import torch
+    rng = np.random.default_rng(seed)
+    x = rng.normal(0, 1.5, (n, Mlp.N_FEATURES)).astype(np.float32)
+    x[:, 0] = 1.0
+    bits = (x.view(np.uint32) + 0x7FFF + ((x.view(np.uint32) >> 16) & 1)) >> 16  # round to bf16
+    xd = torch.as_tensor(bits.astype(np.uint16).view(np.int16), device="cuda")
+    td = torch.as_tensor(rng.normal(0, 1, (n, Mlp.N_OUT)).astype(np.float32), device="cuda")
+    yd = torch.zeros((n, Mlp.N_OUT), device="cuda")
+    m = Mlp(seed=seed + 1)
+    for _ in range(3):
+        m.forward(xd, yd, n)
+        m.train_step(xd, td, n, lr=1e-3)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        e1.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    fwd = timed(lambda: m.forward(xd, yd, n))
+    grd = timed(lambda: m.gradient(xd, td, n))
+    m.close()
+    flops_f = 2 * n * (48 * 64 + 64 * 64 + 64 * 16)
+    flops_g = flops_f + 2 * n * (16 * 64 + 64 * 64) + 2 * n * 128 * (16 + 64 + 64)
+    return {"rows": n, "forward_ms": fwd, "forward_feature_gbs": n * 96 / fwd / 1e6,
+            "forward_tflops": flops_f / fwd / 1e9, "gradient_ms": grd, "gradient_tflops": flops_g / grd / 1e9}
 
 
 if __name__ == "__main__":
