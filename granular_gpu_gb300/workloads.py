@@ -138,6 +138,64 @@ def column_collapse(counts=(128, 256, 256), r=0.002, seed=42, substeps=4, iters=
                  skip)
 
 
+def ramp_walls(space_size, cell_length, angle_deg=30.0, x0=None, x1=None):
+    """Wall particles of an inclined plane across the box (z fills the box):
+    a lattice as fine as the box walls (half a cell), rising at `angle_deg`
+    from the floor at x0 (default: half the box) to x1 (default: the far
+    wall).  The reference builds every obstacle from wall particles
+    (main.cu:849-1167), so a ramp is one more particle set."""
+    sp = np.asarray(space_size, np.float64)
+    h = float(cell_length) / 2.0
+    floor = 0.005 * sp[1]
+    x0 = 0.5 * sp[0] if x0 is None else x0
+    x1 = 0.995 * sp[0] if x1 is None else x1
+    t = math.tan(math.radians(angle_deg))
+    length = (x1 - x0) / math.cos(math.radians(angle_deg))
+    nu = max(2, int(math.ceil(length / h)) + 1)
+    nz = max(2, int(math.ceil(0.99 * sp[2] / h)) + 1)
+    u = np.linspace(0.0, x1 - x0, nu)
+    z = np.linspace(0.005 * sp[2], 0.995 * sp[2], nz)
+    U, Z = np.meshgrid(u, z, indexing="ij")
+    pts = np.stack([x0 + U, floor + U * t, Z], -1).reshape(-1, 3)
+    keep = pts[:, 1] <= 0.995 * sp[1]
+    return pts[keep].astype(np.float32)
+
+
+def adaptive_pile(counts=(64, 64, 64), r=0.005, seed=42, substeps=1, iters=5, upsample_per=4, ledger=1,
+                  max_mass=8.0, origin=None, scaled=False):
+    """The adaptive-pile configuration: fine particles of radius r in a
+    jittered block at spacing 2r (64^3 = 262,144 particles fill a 0.64 m
+    block: the 0.6 x 0.4 x 0.6 m block of the configuration holds only
+    144,000 at that spacing), released 0.02 above the floor of a 2 x 1 x 1
+    box at its -x end, with a 30 degree ramp of wall particles over the +x
+    half; merge/split up to mass `max_mass` (levels 1/2/4/8) on the integer
+    ledger; `upsample_per` render points per particle; dt = 1/240.
+
+    The reference's length constants (wall reach 0.01 + max(r, 0.01), merge
+    radius 0.035, upsampling support 0.045, ...) are kept as compiled in,
+    as the reference would run this scene (`scaled=True` scales them by
+    r / 0.01 instead).  Scaled, the wall reach drops to 2r while the wall
+    particles stay half a cell apart, and a pile this tall presses most
+    particles through the one-particle-thick floor."""
+    L = np.float32(CELL_PER_RADIUS * r)
+    space = (2.0, 1.0, 1.0)
+    walls, cs = box_walls(space, L)
+    walls = np.concatenate([walls, ramp_walls(space, L, 30.0)]).astype(np.float32)
+    floor = 0.005 * space[1]
+    if origin is None:
+        origin = (0.05, floor + 0.01 * (r / 0.01) + r + 0.02, 0.5 - (counts[2] - 1) * r)
+    p = lattice(counts, 2 * r, origin, 0.05 * r, seed)
+    dt = 1.0 / 240.0 / substeps
+    params = scaled_params(r if scaled else REF_RADIUS, iters=iters, dt_sub=None, max_mass=max_mass, ledger=ledger)
+    params.upsample_enabled = 1 if upsample_per else 0
+    params.merge_enabled = 1
+    ups = None
+    if upsample_per:
+        rng = np.random.default_rng(seed + 1)
+        ups = (np.repeat(p, upsample_per, 0) + rng.uniform(-r, r, (p.shape[0] * upsample_per, 3))).astype(np.float32)
+    return _desc(p, walls, ups, space, L, cs, dt, (0.0, -9.81, 0.0), density_for_radius(r), 1, params)
+
+
 def system_kwargs(desc: dict) -> dict:
     """Keyword arguments of GranularSystem(...) from a workload dict."""
     return dict(particles=desc["particles"], boundary_particles=desc["boundary"],
