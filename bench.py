@@ -170,6 +170,36 @@ def run_reference(args):
     return 0
 
 
+def pile_rate(device: int, steps: int) -> dict:
+    import torch
+    import granular_gpu_gb300 as gg
+    from granular_gpu_gb300 import workloads
+    desc = workloads.adaptive_pile()
+    s = gg.GranularSystem(**workloads.system_kwargs(desc), device=device)
+    s.step(100)
+    s.synchronize()
+    st = torch.cuda.ExternalStream(s.stream, device=device)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    units = 0
+    e0.record(st)
+    for _ in range(steps):
+        units += s.size()
+        s.step(1)
+    e1.record(st)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    stats = s.stats()
+    s.close()
+    return {"metric": METRIC, "value": units / (ms / 1e3), "ms_per_step": ms / steps, "steps": steps,
+            "particles_start": desc["n_particles"], "particles_now": stats["n_particles"],
+            "render_points": desc["n_upsampled"], "merged_total": stats["merged_total"],
+            "split_total": stats["split_total"],
+            "mass_units_conserved": stats["total_mass_units"] == desc["n_particles"] * (1 << 20),
+            "workload": "64^3 block (r = 0.005, spacing 2r) dropped 0.02 onto the floor of a 2x1x1 box with a "
+                        "30-degree ramp of wall particles, dt = 1/240, 3+5 sweeps, merge/split to mass 8, "
+                        "4 render points per particle, the reference's length constants; timed after 100 substeps"}
+
+
 def run_mine(args):
     import torch
     import granular_gpu_gb300 as gg
@@ -303,6 +333,12 @@ def run_mine(args):
         "gpu_launches": int(launches),
         "clocks": clocks,
     }
+    if rank == 0 and world == 1 and not args.no_pile:
+        # the adaptive-pile configuration: 262,144 particles of r = 0.005 on the
+        # floor of a box with a 30-degree ramp, merge/split to mass 8 on the
+        # integer ledger, 4 render points per particle; timed after 100
+        # substeps (merges under way)
+        line["adaptive_pile"] = pile_rate(local, args.pile_steps)
     if rank == 0 and world == 1 and not args.no_batched:
         # batched scenes: 64 scenes in one system, autotuned, replayed as a
         # CUDA graph, against the same scenes stepped one after another
@@ -351,6 +387,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-pile", action="store_true")
+    ap.add_argument("--pile-steps", type=int, default=60)
     ap.add_argument("--batched-frames", type=int, default=10)
     ap.add_argument("--learned-frames", type=int, default=150)
     ap.add_argument("--counts", default="128,256,256",

@@ -15,6 +15,17 @@ namespace gg {
 
 // ------------------------------------------------------------ surface
 
+// Prefilter of the neighbour test |d| <= 2 (r_i + r_j) with the surface-law
+// radius r_j: the contact radius in pos.w is never smaller (it divides by
+// the density truncated to an integer), so a candidate beyond
+// 2 (r_i + w_j), with a margin far above the roundings of a fused dot
+// product, fails the exact test; it is skipped without loading r_j.
+__device__ __forceinline__ bool far_for_surface(float3 d, float ri, float wj) {
+  const float dd = __fmaf_rn(d.x, d.x, __fmaf_rn(d.y, d.y, __fmul_rn(d.z, d.z)));
+  const float R = 2.0002f * (ri + wj);
+  return dd > R * R;
+}
+
 // find_cover_vector + find_surface (GranularSystem.cu:506-611) fused: the
 // cover vector of i is only needed by i, so one thread makes both passes.
 // The second pass of the reference counts the neighbours within
@@ -38,7 +49,9 @@ __global__ void __launch_bounds__(256) k_surface(Grid g, int n, const float4* __
     const int j1 = cs[k0 + nc];
     for (int j = cs[k0]; j < j1; ++j) {
       if (j == i) continue;
-      const float3 d = sub3(xi, f3(pos[j]));
+      const float4 xj = pos[j];
+      const float3 d = sub3(xi, f3(xj));
+      if (far_for_surface(d, ri, xj.w)) continue;
       if (sqrt_gt(dot3(d, d), 2.0f * (ri + rs[j]))) continue;
       cv = add3(cv, m_normalize3<MM>(d));
       ++nn;
@@ -54,7 +67,9 @@ __global__ void __launch_bounds__(256) k_surface(Grid g, int n, const float4* __
     const int j1 = cs[k0 + nc];
     for (int j = cs[k0]; j < j1; ++j) {
       if (j == i) continue;
-      float3 b = sub3(f3(pos[j]), xi);
+      const float4 xj = pos[j];
+      float3 b = sub3(f3(xj), xi);
+      if (far_for_surface(b, ri, xj.w)) continue;
       if (sqrt_gt(dot3(b, b), 2.0f * (ri + rs[j]))) continue;
       b = m_normalize3<MM>(b);
       if (m_acos<MM>(dot3(b, c)) <= cone) {
@@ -250,6 +265,9 @@ __global__ void __launch_bounds__(256) k_merge_scan(MergeArgs a) {
     const int j1 = min(a.cs[k0 + nc], a.n);
     for (int j = a.cs[k0]; j < j1; ++j) {
       const float3 d = sub3(xi, f3(a.pos[j]));
+      // candidates clearly beyond the merge radius (a fused dot product
+      // against the cut with a margin far above its rounding) add nothing
+      if (__fmaf_rn(d.x, d.x, __fmaf_rn(d.y, d.y, __fmul_rn(d.z, d.z))) > a.merge_r2_cut * 1.0001f) continue;
       const float dd = dot3(d, d);
       // dis < merge radius (as a float) <=> dd below the smallest square
       // whose rounded root reaches it
