@@ -322,3 +322,41 @@ def test_long_run_statistics_follow_reference(kernels):
     print(f"resting kinetic energy: ours {rest['ours']:.4g}, reference {rest[0]:.4g} and {rest[1]:.4g}")
     assert 0.5 <= rest["ours"] / rest[0] <= 2.0
     s.close()
+
+
+@pytest.mark.parametrize("counts", [(64, 128, 128), (128, 256, 256)])
+def test_throughput_against_reference_kernels(kernels, counts):
+    """Substep time of this library against the reference's own kernels
+    (own flags, driven by the harness's host restatement) on the column
+    collapse without merge/split, upsampling on, the reference's constants
+    as compiled in: the benchmark spec asks for at least 1.5x."""
+    import torch
+    desc = workloads.column_collapse(counts=counts, adaptive=0, upsample_per=4)
+    p = workloads.scaled_params(workloads.REF_RADIUS, iters=5)
+    p.upsample_enabled, p.merge_enabled, p.math_mode = 1, 0, 0
+    desc["params"] = p
+    s = gg.GranularSystem(**workloads.system_kwargs(desc), device=0)
+    s.step(2)
+    ref = _ref_from(kernels[True], s, desc)
+    ref.step()
+    K = 3
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(K):
+        ref.step()
+    e1.record()
+    e1.synchronize()
+    ms_ref = e0.elapsed_time(e1) / K
+    st = torch.cuda.ExternalStream(s.stream)
+    s.synchronize()
+    e0.record(st)
+    for _ in range(K):
+        s.step(1)
+    e1.record(st)
+    e1.synchronize()
+    ms_ours = e0.elapsed_time(e1) / K
+    print(f"{desc['n_particles']} particles, {desc['n_upsampled']} render points: reference kernels "
+          f"{ms_ref:.1f} ms per substep, this library {ms_ours:.2f} ms: {ms_ref / ms_ours:.1f}x")
+    assert ms_ref / ms_ours >= 1.5
+    s.close()
