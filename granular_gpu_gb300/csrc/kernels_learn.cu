@@ -1214,3 +1214,49 @@ extern "C" gg_status gg_set_warm_start(gg_system* S, gg_mlp* M) {
   S->mlp = M;
   return GG_OK;
 }
+
+// ------------------------------------------------------------ self-test of the bounded waits
+
+namespace gg {
+
+// One block waits, with the tensor-core kernels' bounded wait, for an
+// mbarrier phase that nothing completes: the wait must give up after
+// `polls` polls, agree across the block and record ERR_TIMEOUT.
+__global__ void k_wait_selftest(uint32_t polls, int* __restrict__ err) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x == 0) {
+    tc::mbar_init(&bar, 1);
+    tc::fence_mbar_init();
+  }
+  __syncthreads();
+  const bool mine = tc::mbar_wait(&bar, 0, polls);
+  const bool ok = __syncthreads_and(mine) != 0;
+  if (!ok && threadIdx.x == 0) atomicOr(err, ERR_TIMEOUT);
+}
+
+}  // namespace gg
+
+extern "C" gg_status gg_selftest_bounded_wait(int32_t device, int32_t polls) {
+  if (polls <= 0 || polls > (1 << 20)) {
+    set_error("gg_selftest_bounded_wait: polls must be in 1..2^20");
+    return GG_ERR_INVALID_ARGUMENT;
+  }
+  GG_CUDA(cudaSetDevice(device));
+  int* err = nullptr;
+  GG_CUDA(cudaMalloc((void**)&err, sizeof(int)));
+  cudaError_t e = cudaMemset(err, 0, sizeof(int));
+  if (e == cudaSuccess) {
+    k_wait_selftest<<<1, 128>>>((uint32_t)polls, err);
+    e = cudaGetLastError();
+  }
+  int h = 0;
+  if (e == cudaSuccess) e = cudaMemcpy(&h, err, sizeof(int), cudaMemcpyDeviceToHost);
+  cudaFree(err);
+  GG_CUDA(e);
+  if (h & ERR_TIMEOUT) {
+    set_error("gg_selftest_bounded_wait: the wait gave up after its poll limit, as designed");
+    return GG_ERR_TIMEOUT;
+  }
+  set_error("gg_selftest_bounded_wait: a phase nothing completes was reported complete");
+  return GG_ERR_CUDA;
+}

@@ -415,6 +415,12 @@ gg_status gg_mlp_gradient(gg_mlp* mlp, const void* d_features, const float* d_ta
 gg_status gg_mlp_train_step(gg_mlp* mlp, const void* d_features, const float* d_targets, int64_t n, float lr,
                             float weight_decay, float* host_loss, void* stream);
 void gg_mlp_destroy(gg_mlp* mlp);
+/* Diagnostic of the failure path of the tensor-core kernels: one block
+ * waits, with their bounded mbarrier wait, for a phase that nothing
+ * completes.  Returns GG_ERR_TIMEOUT when the wait gave up after `polls`
+ * polls (1..2^20, about 0.2 us each) and the error word recorded it, as it
+ * must; the device stays usable.  No counterpart in the reference. */
+gg_status gg_selftest_bounded_wait(int32_t device, int32_t polls);
 /* Attaches a network to a system for gg_params.warm_start = 1 (mlp may be
  * NULL for warm_start = 2) and allocates the warm-start buffers (feature,
  * predicted-position and target arrays: 124 bytes per particle of
