@@ -34,6 +34,21 @@ __device__ __forceinline__ bool far_for_surface(float3 d, float ri, float wj) {
 // (count <= 5 || !vote).  So the count comes from the first pass, a count
 // of at most 5 decides the flag without a second pass, and the second pass
 // stops at the first vote: the flags are the reference's.
+// Marks, in bit b, the candidates c0 + b (b < cn <= 32) that pass the
+// surface-law prefilter, leaving out i itself.
+__device__ __forceinline__ unsigned surface_chunk_mask(const float4* __restrict__ pos, int c0, int cn, int i,
+                                                       float3 xi, float ri) {
+  unsigned mask = 0u;
+#pragma unroll 4
+  for (int b = 0; b < cn; ++b) {
+    const float4 xj = pos[c0 + b];
+    mask |= (far_for_surface(sub3(xi, f3(xj)), ri, xj.w) ? 0u : 1u) << b;
+  }
+  const unsigned self = (unsigned)(i - c0);
+  if (self < 32u) mask &= ~(1u << self);
+  return mask;
+}
+
 template <int MM>
 __global__ void __launch_bounds__(256) k_surface(Grid g, int n, const float4* __restrict__ pos,
                                                  const float* __restrict__ rs, const int32_t* __restrict__ cs,
@@ -41,20 +56,25 @@ __global__ void __launch_bounds__(256) k_surface(Grid g, int n, const float4* __
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const float3 xi = f3(pos[i]);
-  const float ri = rs[i];
   const int3 q = trunc_cell(g, xi);
+  const float ri = rs[i];
   float3 cv = make_float3(0.f, 0.f, 0.f);
   unsigned nn = 0;
+  // Each stencil column is scanned in chunks of 32: the prefilter marks
+  // the candidates that may lie within 2 (r_i + r_j) in a mask, and the
+  // exact test and the sums run over the marked ones in candidate order.
   for_each_stencil_column(g, q, [&](int k0, int nc) {
     const int j1 = cs[k0 + nc];
-    for (int j = cs[k0]; j < j1; ++j) {
-      if (j == i) continue;
-      const float4 xj = pos[j];
-      const float3 d = sub3(xi, f3(xj));
-      if (far_for_surface(d, ri, xj.w)) continue;
-      if (sqrt_gt(dot3(d, d), 2.0f * (ri + rs[j]))) continue;
-      cv = add3(cv, m_normalize3<MM>(d));
-      ++nn;
+    for (int c0 = cs[k0]; c0 < j1; c0 += 32) {
+      unsigned mask = surface_chunk_mask(pos, c0, min(32, j1 - c0), i, xi, ri);
+      while (mask) {
+        const int j = c0 + __ffs(mask) - 1;
+        mask &= mask - 1u;
+        const float3 d = sub3(xi, f3(pos[j]));
+        if (sqrt_gt(dot3(d, d), 2.0f * (ri + rs[j]))) continue;
+        cv = add3(cv, m_normalize3<MM>(d));
+        ++nn;
+      }
     }
   });
   if (nn <= (unsigned)min_nb) {
@@ -65,16 +85,18 @@ __global__ void __launch_bounds__(256) k_surface(Grid g, int n, const float4* __
   bool vote = false;
   for_each_stencil_column_until(g, q, [&](int k0, int nc) {
     const int j1 = cs[k0 + nc];
-    for (int j = cs[k0]; j < j1; ++j) {
-      if (j == i) continue;
-      const float4 xj = pos[j];
-      float3 b = sub3(f3(xj), xi);
-      if (far_for_surface(b, ri, xj.w)) continue;
-      if (sqrt_gt(dot3(b, b), 2.0f * (ri + rs[j]))) continue;
-      b = m_normalize3<MM>(b);
-      if (m_acos<MM>(dot3(b, c)) <= cone) {
-        vote = true;
-        return true;
+    for (int c0 = cs[k0]; c0 < j1; c0 += 32) {
+      unsigned mask = surface_chunk_mask(pos, c0, min(32, j1 - c0), i, xi, ri);
+      while (mask) {
+        const int j = c0 + __ffs(mask) - 1;
+        mask &= mask - 1u;
+        float3 b = sub3(f3(pos[j]), xi);
+        if (sqrt_gt(dot3(b, b), 2.0f * (ri + rs[j]))) continue;
+        b = m_normalize3<MM>(b);
+        if (m_acos<MM>(dot3(b, c)) <= cone) {
+          vote = true;
+          return true;
+        }
       }
     }
     return false;
@@ -261,27 +283,39 @@ __global__ void __launch_bounds__(256) k_merge_scan(MergeArgs a) {
   float ld = 0.0f;
   int lc = 0;
   const bool sd_bug = a.sdist[i] < a.sdt;  // Solver.cu:578 tests [i]: always false here
+  const float pre_cut = a.merge_r2_cut * 1.0001f;
   for_each_stencil_column(a.g, q, [&](int k0, int nc) {
     const int j1 = min(a.cs[k0 + nc], a.n);
-    for (int j = a.cs[k0]; j < j1; ++j) {
-      const float3 d = sub3(xi, f3(a.pos[j]));
+    for (int c0 = a.cs[k0]; c0 < j1; c0 += 32) {
       // candidates clearly beyond the merge radius (a fused dot product
-      // against the cut with a margin far above its rounding) add nothing
-      if (__fmaf_rn(d.x, d.x, __fmaf_rn(d.y, d.y, __fmul_rn(d.z, d.z))) > a.merge_r2_cut * 1.0001f) continue;
-      const float dd = dot3(d, d);
-      // dis < merge radius (as a float) <=> dd below the smallest square
-      // whose rounded root reaches it
-      const bool inr = dd < a.merge_r2_cut;
-      if (inr) {
-        ld += a.mass[j];
-        ++lc;
+      // against the cut with a margin far above its rounding) add nothing:
+      // the chunk's mask marks the others, visited in candidate order
+      const int cn = min(32, j1 - c0);
+      unsigned mask = 0u;
+#pragma unroll 4
+      for (int b = 0; b < cn; ++b) {
+        const float3 d = sub3(xi, f3(a.pos[c0 + b]));
+        mask |= (__fmaf_rn(d.x, d.x, __fmaf_rn(d.y, d.y, __fmul_rn(d.z, d.z))) > pre_cut ? 0u : 1u) << b;
       }
-      if (!inr || j <= i || sd_bug || a.remove[j] != 0 || a.surface[j] != 0) continue;
-      if (mi + a.mass[j] > a.max_mass) continue;
-      const float dis = sqrtf(dd);
-      if (dis < closest) {
-        closest = dis;
-        ci = j;
+      while (mask) {
+        const int j = c0 + __ffs(mask) - 1;
+        mask &= mask - 1u;
+        const float3 d = sub3(xi, f3(a.pos[j]));
+        const float dd = dot3(d, d);
+        // dis < merge radius (as a float) <=> dd below the smallest square
+        // whose rounded root reaches it
+        const bool inr = dd < a.merge_r2_cut;
+        if (inr) {
+          ld += a.mass[j];
+          ++lc;
+        }
+        if (!inr || j <= i || sd_bug || a.remove[j] != 0 || a.surface[j] != 0) continue;
+        if (mi + a.mass[j] > a.max_mass) continue;
+        const float dis = sqrtf(dd);
+        if (dis < closest) {
+          closest = dis;
+          ci = j;
+        }
       }
     }
   });
