@@ -33,16 +33,38 @@ int key_bits(int C) {
 
 // mapParticles2Cells_CUDA (CUDAFunctions.cuh:91-107) with the sort's value
 // array (thrust::sequence, GranularSystem.cu:71-73) produced in one pass.
-__global__ void k_hash(Grid g, const float4* __restrict__ pos, int n, uint32_t* __restrict__ keys,
-                       uint32_t* __restrict__ vals, uint32_t* __restrict__ keys_copy) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const float4 p = pos[i];
-  const int3 c = floor_cell(g, make_float3(p.x, p.y, p.z));
-  const uint32_t k = (uint32_t)cell_key(g, c.x, c.y, c.z);
-  keys[i] = k;
-  vals[i] = (uint32_t)i;
-  if (keys_copy) keys_copy[i] = k;
+// One block per sort tile: the block also counts the tile's first radix
+// digits (bits 0-7), hist0 digit-major [256][tiles], so the sort's first
+// pass does not read the keys again for its histogram.
+__global__ void __launch_bounds__(kSortThreads) k_hash(Grid g, const float4* __restrict__ pos, int n,
+                                                       uint32_t* __restrict__ keys, uint32_t* __restrict__ vals,
+                                                       uint32_t* __restrict__ keys_copy, int tiles,
+                                                       uint32_t* __restrict__ hist0) {
+  __shared__ uint32_t h[256];
+  h[threadIdx.x] = 0;
+  __syncthreads();
+  const int base = blockIdx.x * kSortTile;
+  const unsigned lt = lanemask_lt();
+#pragma unroll 4
+  for (int r = 0; r < kSortItems; ++r) {
+    const int i = base + r * kSortThreads + threadIdx.x;
+    uint32_t d = 0u;
+    if (i < n) {
+      const float4 p = pos[i];
+      const int3 c = floor_cell(g, make_float3(p.x, p.y, p.z));
+      const uint32_t k = (uint32_t)cell_key(g, c.x, c.y, c.z);
+      keys[i] = k;
+      vals[i] = (uint32_t)i;
+      if (keys_copy) keys_copy[i] = k;
+      d = k & 255u;
+    }
+    // one shared-memory atomic per distinct digit of the warp (sorted or
+    // nearly sorted keys share their digit across the warp)
+    const unsigned peers = __match_any_sync(0xffffffffu, i < n ? d : 256u);
+    if (i < n && (peers & lt) == 0) atomicAdd(&h[d], (uint32_t)__popc(peers));
+  }
+  __syncthreads();
+  hist0[threadIdx.x * tiles + blockIdx.x] = h[threadIdx.x];
 }
 
 // ------------------------------------------------------------ block scan
@@ -153,62 +175,84 @@ gg_status exclusive_scan(const int32_t* in, int32_t* out, int64_t n, SortScratch
 // ------------------------------------------------------------ radix sort
 
 // Per-tile histogram of one 8-bit digit; hist is digit-major [256][tiles].
-__global__ void k_radix_hist(const uint32_t* __restrict__ keys, int n, int shift, int tiles,
-                             uint32_t* __restrict__ hist) {
+// The thread's 16 keys are loaded before any is counted, so that their
+// loads are in flight together; counts are aggregated over the lanes of a
+// warp holding the same digit (one shared-memory atomic per digit).
+__global__ void __launch_bounds__(kSortThreads) k_radix_hist(const uint32_t* __restrict__ keys, int n, int shift,
+                                                             int tiles, uint32_t* __restrict__ hist) {
   __shared__ uint32_t h[256];
   h[threadIdx.x] = 0;
-  __syncthreads();
   const int base = blockIdx.x * kSortTile;
-#pragma unroll 4
+  uint32_t k[kSortItems];
+#pragma unroll
   for (int r = 0; r < kSortItems; ++r) {
     const int i = base + r * kSortThreads + threadIdx.x;
-    if (i < n) atomicAdd(&h[(keys[i] >> shift) & 255u], 1u);
+    k[r] = i < n ? keys[i] : 0u;
+  }
+  __syncthreads();
+  const unsigned lt = lanemask_lt();
+#pragma unroll
+  for (int r = 0; r < kSortItems; ++r) {
+    const bool valid = base + r * kSortThreads + (int)threadIdx.x < n;
+    const uint32_t d = (k[r] >> shift) & 255u;
+    const unsigned peers = __match_any_sync(0xffffffffu, valid ? d : 256u);
+    if (valid && (peers & lt) == 0) atomicAdd(&h[d], (uint32_t)__popc(peers));
   }
   __syncthreads();
   hist[threadIdx.x * tiles + blockIdx.x] = h[threadIdx.x];
 }
 
-// Stable scatter: items are ranked in index order within the tile (rounds
-// of 256 consecutive items; within a round by warp, then by lane).
-__global__ void k_radix_scatter(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin,
-                                uint32_t* __restrict__ kout, uint32_t* __restrict__ vout, int n,
-                                int shift, int tiles, const uint32_t* __restrict__ offs) {
+// Stable scatter of one digit: items are ranked in index order within the
+// tile (rounds of 256 consecutive items; within a round by warp, then by
+// lane).  offs holds the exclusive scan of the digit-major [256][tiles]
+// histogram.  The thread's 16 keys and values are loaded before the first
+// round, so that the rounds wait on no global load.  In a round, the first
+// lane of each group of equal digits in a warp posts the group's size in
+// wcnt; after the writes it adds the size to the digit's running base and
+// clears its entry, so that wcnt is all zero between rounds.
+__global__ void __launch_bounds__(kSortThreads) k_radix_scatter(const uint32_t* __restrict__ kin,
+                                                                const uint32_t* __restrict__ vin,
+                                                                uint32_t* __restrict__ kout,
+                                                                uint32_t* __restrict__ vout, int n, int shift,
+                                                                int tiles, const uint32_t* __restrict__ offs) {
   constexpr int W = kSortThreads / 32;
   __shared__ uint32_t base_d[256];
   __shared__ uint32_t wcnt[W][256];
   const int t = threadIdx.x, warp = t >> 5;
-  base_d[t] = offs[t * tiles + blockIdx.x];
   const int base = blockIdx.x * kSortTile;
-  const unsigned lt = lanemask_lt();
+  uint32_t k[kSortItems], v[kSortItems];
+#pragma unroll
   for (int r = 0; r < kSortItems; ++r) {
-#pragma unroll
-    for (int w = 0; w < W; ++w) wcnt[w][t] = 0;
-    __syncthreads();
     const int i = base + r * kSortThreads + t;
-    const bool valid = i < n;
-    uint32_t k = 0, v = 0, d = 256;
-    if (valid) {
-      k = kin[i];
-      v = vin[i];
-      d = (k >> shift) & 255u;
-    }
-    const unsigned peers = __match_any_sync(0xffffffffu, d);
-    const int rank = __popc(peers & lt);
-    if (valid && rank == 0) wcnt[warp][d] = __popc(peers);
-    __syncthreads();
-    if (valid) {
-      uint32_t pre = 0;
-      for (int w = 0; w < warp; ++w) pre += wcnt[w][d];
-      const uint32_t dst = base_d[d] + pre + rank;
-      kout[dst] = k;
-      vout[dst] = v;
-    }
-    __syncthreads();
-    uint32_t tot = 0;
+    k[r] = i < n ? kin[i] : 0u;
+    v[r] = i < n ? vin[i] : 0u;
+  }
 #pragma unroll
-    for (int w = 0; w < W; ++w) tot += wcnt[w][t];
-    base_d[t] += tot;
+  for (int w = 0; w < W; ++w) wcnt[w][t] = 0;
+  base_d[t] = offs[t * tiles + blockIdx.x];
+  __syncthreads();
+  const unsigned lt = lanemask_lt();
+#pragma unroll
+  for (int r = 0; r < kSortItems; ++r) {
+    const bool valid = base + r * kSortThreads + t < n;
+    const uint32_t d = (k[r] >> shift) & 255u;
+    const unsigned peers = __match_any_sync(0xffffffffu, valid ? d : 256u);
+    const bool leader = valid && (peers & lt) == 0;
+    const uint32_t cnt = (uint32_t)__popc(peers);
+    if (leader) wcnt[warp][d] = cnt;
     __syncthreads();
+    if (valid) {
+      uint32_t dst = base_d[d] + (uint32_t)__popc(peers & lt);
+      for (int w = 0; w < warp; ++w) dst += wcnt[w][d];
+      kout[dst] = k[r];
+      vout[dst] = v[r];
+    }
+    __syncthreads();
+    if (leader) {
+      atomicAdd(&base_d[d], cnt);
+      wcnt[warp][d] = 0;
+    }
+    __syncwarp();
   }
 }
 
@@ -241,9 +285,10 @@ void sort_scratch_free(SortScratch& s) {
 }
 
 // Stable LSD sort of the (key, value) pairs held in s.k[0], s.v[0]; the
-// last pass writes keys_out / perm_out.
+// last pass writes keys_out / perm_out.  hist0_ready: s.hist already holds
+// the first digit's tile histogram (counted by the hash kernel).
 static gg_status radix_sort_pairs(const Grid& g, int64_t n, SortScratch& s, uint32_t* keys_out, uint32_t* perm_out,
-                                  cudaStream_t st) {
+                                  cudaStream_t st, bool hist0_ready) {
   const int nn = (int)n;
   const int bits = key_bits(g.C);
   const int passes = (bits + 7) / 8;
@@ -254,11 +299,14 @@ static gg_status radix_sort_pairs(const Grid& g, int64_t n, SortScratch& s, uint
     const bool last = p == passes - 1;
     uint32_t* ko = last ? keys_out : s.k[src ^ 1];
     uint32_t* vo = last ? perm_out : s.v[src ^ 1];
-    k_radix_hist<<<tiles, kSortThreads, 0, st>>>(s.k[src], nn, shift, tiles, s.hist);
+    if (p > 0 || !hist0_ready) {
+      k_radix_hist<<<tiles, kSortThreads, 0, st>>>(s.k[src], nn, shift, tiles, s.hist);
+      if (s.counter) *s.counter += 1;
+    }
     gg_status rc = exclusive_scan((const int32_t*)s.hist, (int32_t*)s.hist, (int64_t)tiles * 256, s, st, nullptr);
     if (rc != GG_OK) return rc;
     k_radix_scatter<<<tiles, kSortThreads, 0, st>>>(s.k[src], s.v[src], ko, vo, nn, shift, tiles, s.hist);
-    if (s.counter) *s.counter += 2;
+    if (s.counter) *s.counter += 1;
     src ^= 1;
   }
   GG_CUDA(cudaGetLastError());
@@ -274,11 +322,12 @@ gg_status grid_sort(const Grid& g, const float4* pos, int64_t n, SortScratch& s,
   }
   const int nn = (int)n;
   if (prof) prof_begin(prof, PC_HASH, st);
-  k_hash<<<blocks_for(n, 256), 256, 0, st>>>(g, pos, nn, s.k[0], s.v[0], keys_unsorted_out);
+  const int tiles = (int)((n + kSortTile - 1) / kSortTile);
+  k_hash<<<tiles, kSortThreads, 0, st>>>(g, pos, nn, s.k[0], s.v[0], keys_unsorted_out, tiles, s.hist);
   if (s.counter) *s.counter += 1;
   if (prof) prof_end(prof, PC_HASH, n, st);
   if (prof) prof_begin(prof, PC_SORT, st);
-  gg_status rc = radix_sort_pairs(g, n, s, keys_out, perm_out, st);
+  gg_status rc = radix_sort_pairs(g, n, s, keys_out, perm_out, st, true);
   if (prof) prof_end(prof, PC_SORT, n, st);
   return rc;
 }
@@ -503,7 +552,7 @@ extern "C" gg_status gg_grid_build_noalloc(int32_t device, const float* d_pos, i
     if (n > 0) {
       k_hash3<<<blocks_for(n, 256), 256, 0, st>>>(g, d_pos, (int)n, s.k[0], s.v[0]);
       GG_CUDA(cudaGetLastError());
-      rc = radix_sort_pairs(g, n, s, d_sorted_keys, d_perm, st);
+      rc = radix_sort_pairs(g, n, s, d_sorted_keys, d_perm, st, false);
       if (rc != GG_OK) return rc;
     }
     // cell_start_build clears the caller's table (the counts start at zero)
