@@ -85,6 +85,7 @@ struct Granular {
   uint32_t* keys = nullptr;   // sorted keys of the last build
   uint32_t* perm = nullptr;   // sort permutation of the last build
   int32_t* cell_start = nullptr;
+  uint8_t* cell_surf = nullptr;  // C + 1: cell holds a surface particle (scratch of the surface distance)
   // adaptive scratch
   int32_t* prop = nullptr;
   float* ldens = nullptr;

@@ -169,10 +169,22 @@ gg_status surface(gg_system* S, cudaStream_t st) {
   return GG_OK;
 }
 
-// compute_distance_to_surface, GranularSystem.cu:639-688.
+// Marks the cells that hold a surface particle (by binning key).
+__global__ void k_mark_surface_cells(int n, int C, const int32_t* __restrict__ surface,
+                                     const uint32_t* __restrict__ keys, uint8_t* __restrict__ cell_surf) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t k = keys[i];
+  if (surface[i] != 0 && k < (uint32_t)C) cell_surf[k] = 1;
+}
+
+// compute_distance_to_surface, GranularSystem.cu:639-688.  The result is a
+// minimum, so the visiting order does not matter, and cells without a
+// surface particle (cell_surf 0) hold no candidate: they are skipped.
 __global__ void __launch_bounds__(256) k_surfdist(Grid g, int n, const float4* __restrict__ pos,
                                                   const int32_t* __restrict__ surface,
-                                                  const int32_t* __restrict__ cs, float* __restrict__ sdist,
+                                                  const int32_t* __restrict__ cs,
+                                                  const uint8_t* __restrict__ cell_surf, float* __restrict__ sdist,
                                                   float none) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -183,14 +195,16 @@ __global__ void __launch_bounds__(256) k_surfdist(Grid g, int n, const float4* _
   const float3 xi = f3(pos[i]);
   const int3 q = trunc_cell(g, xi);
   float best = none;
-  // a minimum: the visiting order does not matter
   for_each_stencil_column(g, q, [&](int k0, int nc) {
-    const int j1 = cs[k0 + nc];
-    for (int j = cs[k0]; j < j1; ++j) {
-      if (j == i || surface[j] == 0) continue;
-      const float3 d = sub3(xi, f3(pos[j]));
-      const float d2 = dot3(d, d);
-      if (d2 < best) best = d2;
+    for (int z = 0; z < nc; ++z) {
+      if (!cell_surf[k0 + z]) continue;
+      const int j1 = cs[k0 + z + 1];
+      for (int j = cs[k0 + z]; j < j1; ++j) {
+        if (j == i || surface[j] == 0) continue;
+        const float3 d = sub3(xi, f3(pos[j]));
+        const float d2 = dot3(d, d);
+        if (d2 < best) best = d2;
+      }
     }
   });
   sdist[i] = best;
@@ -233,10 +247,19 @@ __global__ void __launch_bounds__(256) k_surfdist_warp(Grid g, int n, const floa
 gg_status surface_distance(gg_system* S, cudaStream_t st) {
   if (S->n <= 0) return GG_OK;
   prof_begin(S, PC_SURFDIST, st);
-  auto kern = S->P.reserved[1] != 1 ? k_surfdist : k_surfdist_warp;
-  kern<<<blocks_for(S->n, 256), 256, 0, st>>>(S->grid, (int)S->n, S->g.pos[S->g.cur], S->g.surface,
-                                                    S->g.cell_start, S->g.sdist, S->P.no_surface_distance);
-  count_launches(S, 1);
+  if (S->P.reserved[1] != 1) {
+    GG_CUDA(cudaMemsetAsync(S->g.cell_surf, 0, (size_t)S->grid.C + 1, st));
+    k_mark_surface_cells<<<blocks_for(S->n, 256), 256, 0, st>>>((int)S->n, S->grid.C, S->g.surface, S->g.keys,
+                                                                S->g.cell_surf);
+    k_surfdist<<<blocks_for(S->n, 256), 256, 0, st>>>(S->grid, (int)S->n, S->g.pos[S->g.cur], S->g.surface,
+                                                      S->g.cell_start, S->g.cell_surf, S->g.sdist,
+                                                      S->P.no_surface_distance);
+    count_launches(S, 2);
+  } else {
+    k_surfdist_warp<<<blocks_for(S->n, 256), 256, 0, st>>>(S->grid, (int)S->n, S->g.pos[S->g.cur], S->g.surface,
+                                                           S->g.cell_start, S->g.sdist, S->P.no_surface_distance);
+    count_launches(S, 1);
+  }
   prof_end(S, PC_SURFDIST, S->n, st);
   GG_CUDA(cudaGetLastError());
   return GG_OK;

@@ -208,7 +208,7 @@ static void free_all(gg_system* S) {
     cudaFree(S->u.pos[k]); cudaFree(S->u.vel[k]);
   }
   void* ptrs[] = {G.merge_vel, G.surface, G.sdist, G.cover, G.xs, G.inv_m, G.delta, G.s_extra, G.contacts,
-                  G.ncon, G.keys, G.perm, G.cell_start, G.prop, G.ldens, G.winner, G.split_flag, G.keep_flag,
+                  G.ncon, G.keys, G.perm, G.cell_start, G.cell_surf, G.prop, G.ldens, G.winner, G.split_flag, G.keep_flag,
                   G.split_slot, G.keep_slot, G.child_pos, G.nl_idx, G.nl_meta, G.nl_acc, G.nl_queue, G.cell_inc, S->b.pos, S->b.animated, S->b.pos_alt,
                   S->b.animated_alt, S->b.keys, S->b.perm, S->b.cell_start, S->u.keys, S->u.perm, S->scal,
                   S->stats_partial, S->stage, S->feat, S->xs0, S->warm_target, S->scene_fcap,
@@ -309,7 +309,7 @@ gg_status system_create(const gg_desc* d, gg_system** out) {
   ALLOC(G.merge_vel, cap); ALLOC(G.surface, cap); ALLOC(G.sdist, cap); ALLOC(G.cover, cap);
   ALLOC(G.xs, cap); ALLOC(G.inv_m, cap); ALLOC(G.delta, cap); ALLOC(G.s_extra, cap);
   ALLOC(G.contacts, cap); ALLOC(G.ncon, cap); ALLOC(G.keys, cap); ALLOC(G.perm, cap);
-  ALLOC(G.cell_start, C1); ALLOC(G.prop, cap); ALLOC(G.ldens, cap); ALLOC(G.winner, cap);
+  ALLOC(G.cell_start, C1); ALLOC(G.cell_surf, C1); ALLOC(G.prop, cap); ALLOC(G.ldens, cap); ALLOC(G.winner, cap);
   ALLOC(G.split_flag, cap); ALLOC(G.keep_flag, cap); ALLOC(G.split_slot, cap); ALLOC(G.keep_slot, cap);
   ALLOC(G.child_pos, cap);
   // contact lists: a negative skin asks for the automatic one, a tenth of
