@@ -872,14 +872,26 @@ __global__ void __launch_bounds__(kBuildThreads) k_sweep_nlist_build(SweepArgs a
       if (cnt < kNlistMax) s_list[w][cnt][lane] = e;
       ++cnt;
     };
+    // candidates in chunks of 32: a mask of those within reach, then the
+    // pushes in index order
     auto scan_particles = [&](int j0, int j1) {
+      for (int c0 = j0; c0 < j1; c0 += 32) {
+        const int cn = min(32, j1 - c0);
+        unsigned mask = 0u;
 #pragma unroll 4
-      for (int j = j0; j < j1; ++j) {
-        const float4 xj = a.xs[j];
-        const float dx = t.x.x - xj.x, dy = t.x.y - xj.y, dz = t.x.z - xj.z;
-        const float rs = rcs + xj.w;
-        const float d2 = __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmul_rn(dz, dz)));
-        if (!(d2 > rs * rs * 1.0001f) && j != i) push(j);
+        for (int b = 0; b < cn; ++b) {
+          const float4 xj = a.xs[c0 + b];
+          const float dx = t.x.x - xj.x, dy = t.x.y - xj.y, dz = t.x.z - xj.z;
+          const float rs = rcs + xj.w;
+          const float d2 = __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmul_rn(dz, dz)));
+          mask |= (d2 > rs * rs * 1.0001f ? 0u : 1u) << b;
+        }
+        const unsigned self = (unsigned)(i - c0);
+        if (self < 32u) mask &= ~(1u << self);
+        while (mask) {
+          push(c0 + __ffs(mask) - 1);
+          mask &= mask - 1u;
+        }
       }
     };
     for_each_stencil_column(g, t.q, [&](int k0, int nc) {
