@@ -49,6 +49,10 @@ __device__ __forceinline__ unsigned surface_chunk_mask(const float4* __restrict_
   return mask;
 }
 
+// The nine stencil columns (x, y offsets in units of the signs of the cover
+// vector's x and y), most aligned with it first.
+__constant__ int kTowards[9][2] = {{1, 1}, {1, 0}, {0, 1}, {0, 0}, {1, -1}, {-1, 1}, {0, -1}, {-1, 0}, {-1, -1}};
+
 template <int MM>
 __global__ void __launch_bounds__(256) k_surface(Grid g, int n, const float4* __restrict__ pos,
                                                  const float* __restrict__ rs, const int32_t* __restrict__ cs,
@@ -82,25 +86,46 @@ __global__ void __launch_bounds__(256) k_surface(Grid g, int n, const float4* __
     return;
   }
   const float3 c = m_normalize3<MM>(cv);
+  // The vote is an OR over the neighbours, so the order they are visited in
+  // is free: the stencil columns towards c first, and within a column from
+  // the end c.z points to, so that an interior particle meets a neighbour
+  // inside the cone early.  acos(d) <= cone is decided from d alone away
+  // from cos(cone) (the margin of 1e-5 on d is some 40 times the bound on
+  // acosf's error there); near it acos is evaluated.
+  const float cos_cone = cosf(cone);
+  const float d_in = cos_cone + 1e-5f, d_out = cos_cone - 1e-5f;
+  const int sx = c.x < 0.0f ? -1 : 1, sy = c.y < 0.0f ? -1 : 1;
+  const bool up = c.z > 0.0f;
+  // (64-bit cell coordinates: q saturates for positions far outside the grid)
+  const long long zl = max((long long)q.z - 1, 0LL), zh = min((long long)q.z + 1, (long long)g.nz - 1);
   bool vote = false;
-  for_each_stencil_column_until(g, q, [&](int k0, int nc) {
-    const int j1 = cs[k0 + nc];
-    for (int c0 = cs[k0]; c0 < j1; c0 += 32) {
-      unsigned mask = surface_chunk_mask(pos, c0, min(32, j1 - c0), i, xi, ri);
-      while (mask) {
-        const int j = c0 + __ffs(mask) - 1;
-        mask &= mask - 1u;
-        float3 b = sub3(f3(pos[j]), xi);
-        if (sqrt_gt(dot3(b, b), 2.0f * (ri + rs[j]))) continue;
-        b = m_normalize3<MM>(b);
-        if (m_acos<MM>(dot3(b, c)) <= cone) {
-          vote = true;
-          return true;
+  if (zl <= zh) {
+    for (int o = 0; o < 9 && !vote; ++o) {
+      const long long x = (long long)q.x + sx * kTowards[o][0], y = (long long)q.y + sy * kTowards[o][1];
+      if (x < 0 || x >= g.nx || y < 0 || y >= g.ny) continue;
+      const int k0 = (int)((x * g.ny + y) * g.nz + zl);
+      const int j0 = cs[k0], j1 = cs[k0 + (int)(zh - zl + 1)];
+      const int nch = (j1 - j0 + 31) >> 5;
+      for (int ch = 0; ch < nch && !vote; ++ch) {
+        const int c0 = j0 + 32 * (up ? nch - 1 - ch : ch);
+        unsigned mask = surface_chunk_mask(pos, c0, min(32, j1 - c0), i, xi, ri);
+        while (mask) {
+          const int bit = up ? 31 - __clz(mask) : __ffs(mask) - 1;
+          mask &= ~(1u << bit);
+          const int j = c0 + bit;
+          float3 b = sub3(f3(pos[j]), xi);
+          if (sqrt_gt(dot3(b, b), 2.0f * (ri + rs[j]))) continue;
+          b = m_normalize3<MM>(b);
+          const float d = dot3(b, c);
+          const bool in = d > d_in ? true : (d < d_out ? false : m_acos<MM>(d) <= cone);
+          if (in) {
+            vote = true;
+            break;
+          }
         }
       }
     }
-    return false;
-  });
+  }
   surface[i] = vote ? 0 : 1;
 }
 
