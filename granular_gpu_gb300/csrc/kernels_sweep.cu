@@ -235,8 +235,11 @@ __device__ __forceinline__ void particle_pair_f(const SweepArgs& a, const Target
   }
   ++c;
   const int3 qj = trunc_cell(a.g, make_float3(xj4.x, xj4.y, xj4.z));
-  const bool j_finds_i = t.binned && llabs((long long)t.cx - qj.x) <= 1 && llabs((long long)t.cy - qj.y) <= 1 &&
-                         llabs((long long)t.cz - qj.z) <= 1;
+  // |c - qj| <= 1 per axis, as one unsigned window test: c is a binning
+  // cell (0 <= c < n < 2^31), so c + 1 - qj stays below 2^32 for every int
+  // qj and lies in [0, 2] exactly when qj is within one cell of c.
+  const bool j_finds_i = t.binned && (unsigned)t.cx + 1u - (unsigned)qj.x <= 2u &&
+                         (unsigned)t.cy + 1u - (unsigned)qj.y <= 2u && (unsigned)t.cz + 1u - (unsigned)qj.z <= 2u;
   if (j_finds_i) ++s_loc;
   else atomicAdd(&a.s_extra[j], 1);
 }
