@@ -296,13 +296,27 @@ bool field_view(gg_system* S, gg_set set, gg_field f, FieldView& v) {
   return false;
 }
 
-// Device float4 fields cross to the host as packed float[3]: a kernel packs
-// them into the staging buffer and one contiguous copy moves them (a pitched
-// copy with 12-byte rows runs far below the link's bandwidth).
+// The device address of pinned (page-locked, mapped) host memory, or null
+// for memory the device cannot address directly.
+void* mapped_host(const void* host) {
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, host) != cudaSuccess) {
+    cudaGetLastError();  // unregistered memory on older runtimes
+    return nullptr;
+  }
+  return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
+
+// Device float4 fields cross to the host as packed float[3].  Pinned host
+// buffers are written (read) by the packing kernel itself over the
+// host-device link; other buffers go through the device staging buffer and
+// one contiguous copy (a pitched copy with 12-byte rows runs far below the
+// link's bandwidth).
 cudaError_t copy_out(gg_system* S, const FieldView& v, void* dst, int64_t count, cudaStream_t st) {
   if (count <= 0) return cudaSuccess;
   if (v.elem == v.stride)
     return cudaMemcpyAsync(dst, v.ptr, (size_t)v.elem * count, cudaMemcpyDeviceToHost, st);
+  if (void* mapped = mapped_host(dst)) return pack3(S, (const float4*)v.ptr, (float*)mapped, count, st);
   cudaError_t e = pack3(S, (const float4*)v.ptr, S->stage, count, st);
   if (e != cudaSuccess) return e;
   return cudaMemcpyAsync(dst, S->stage, (size_t)12 * count, cudaMemcpyDeviceToHost, st);
@@ -312,6 +326,7 @@ cudaError_t copy_in(gg_system* S, const FieldView& v, const void* src, int64_t c
   if (count <= 0) return cudaSuccess;
   if (v.elem == v.stride)
     return cudaMemcpyAsync(v.ptr, src, (size_t)v.elem * count, cudaMemcpyHostToDevice, st);
+  if (void* mapped = mapped_host(src)) return unpack3(S, (const float*)mapped, (float4*)v.ptr, count, st);
   cudaError_t e = cudaMemcpyAsync(S->stage, src, (size_t)12 * count, cudaMemcpyHostToDevice, st);
   if (e != cudaSuccess) return e;
   return unpack3(S, S->stage, (float4*)v.ptr, count, st);

@@ -355,3 +355,33 @@ def test_vtk_writer(tmp_path):
     first = [float(v) for v in lines[5].split()]
     assert np.allclose(first, [x[0, 0], x[0, 2], x[0, 1]], rtol=1e-5)
     assert lines[5 + n] == f"CELLS {n} {2 * n}" and lines[6 + 2 * n] == f"CELL_TYPES {n}"
+
+
+def test_host_copies_pinned_misaligned_and_pageable_agree():
+    # pinned buffers are packed by the copy kernel itself, pageable ones go
+    # through the device staging buffer: every path returns and accepts the
+    # same bits, aligned or not, including a partial last block
+    torch = pytest.importorskip("torch")
+    desc = workloads.box_drop(n_side=11, upsample_per=2)
+    s = gg.GranularSystem(**workloads.system_kwargs(desc), device=0)
+    s.step(2)
+    n = s.size()
+    assert n % 256 != 0 and n > 256
+    ref = s.read(gg.FIELD_POS).copy()
+    refu = s.read(gg.FIELD_VEL, gg.SET_UPSAMPLED).copy()
+    pin = torch.empty(3 * n + 1, dtype=torch.float32, pin_memory=True).numpy()
+    aligned, shifted = pin[: 3 * n].reshape(n, 3), pin[1: 3 * n + 1].reshape(n, 3)
+    for buf in (aligned, shifted):
+        buf[:] = 0
+        s.read(gg.FIELD_POS, out=buf)
+        assert np.array_equal(buf, ref)
+    nu = refu.shape[0]
+    upin = torch.empty((nu, 3), dtype=torch.float32, pin_memory=True).numpy()
+    s.read(gg.FIELD_VEL, gg.SET_UPSAMPLED, out=upin)
+    assert np.array_equal(upin, refu)
+    moved = ref + np.float32(1e-3)
+    for buf in (np.array(ref), aligned, shifted):
+        buf[:] = moved
+        s.write(gg.FIELD_POS, buf)
+        assert np.array_equal(s.read(gg.FIELD_POS), moved)
+    s.close()
