@@ -178,6 +178,7 @@ def pile_rate(device: int, steps: int) -> dict:
     s = gg.GranularSystem(**workloads.system_kwargs(desc), device=device)
     s.step(100)
     s.synchronize()
+    tune = s.autotune(2)
     st = torch.cuda.ExternalStream(s.stream, device=device)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     units = 0
@@ -195,9 +196,12 @@ def pile_rate(device: int, steps: int) -> dict:
             "render_points": desc["n_upsampled"], "merged_total": stats["merged_total"],
             "split_total": stats["split_total"],
             "mass_units_conserved": stats["total_mass_units"] == desc["n_particles"] * (1 << 20),
+            "autotune": {k: tune[k] for k in ("sweep_variant", "keep_threads", "build_blocks_per_sm", "trials",
+                                              "ms_default", "ms_tuned")},
             "workload": "64^3 block (r = 0.005, spacing 2r) dropped 0.02 onto the floor of a 2x1x1 box with a "
                         "30-degree ramp of wall particles, dt = 1/240, 3+5 sweeps, merge/split to mass 8, "
-                        "4 render points per particle, the reference's length constants; timed after 100 substeps"}
+                        "4 render points per particle, the reference's length constants; autotuned (gg_autotune) "
+                        "and timed after 100 substeps"}
 
 
 def run_mine(args):

@@ -242,6 +242,13 @@ class GranularSystem:
         _check(lib().gg_set_params(self._h, C.byref(p)))
 
     # -- learned warm start -------------------------------------------------
+    def autotune(self, substeps: int = 2) -> dict:
+        """gg_autotune: the fastest launch shapes and default-sweep variant
+        for this system's current state (the state is left as it was)."""
+        t = abi.gg_tuning()
+        _check(lib().gg_autotune(self._h, substeps, C.byref(t)))
+        return {k: getattr(t, k) for k, _ in abi.gg_tuning._fields_ if k != "pad_"}
+
     def set_warm_start(self, mlp=None):
         """gg_set_warm_start: attach a network (gg_params.warm_start = 1) or,
         with None, only allocate the buffers of the recording mode (2)."""

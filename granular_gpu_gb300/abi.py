@@ -152,7 +152,8 @@ class gg_stats_t(C.Structure):
 class gg_tuning(C.Structure):
     _fields_ = [("predict_threads", C.c_int32), ("apply_threads", C.c_int32), ("finalize_threads", C.c_int32),
                 ("keep_threads", C.c_int32), ("build_blocks_per_sm", C.c_int32), ("trials", C.c_int32),
-                ("ms_default", C.c_float), ("ms_tuned", C.c_float)]
+                ("ms_default", C.c_float), ("ms_tuned", C.c_float), ("sweep_variant", C.c_int32),
+                ("pad_", C.c_int32)]
 
 
 GG_PROF_MAX = 24

@@ -101,9 +101,7 @@ class Batch:
 
     def autotune(self, substeps: int = 4) -> dict:
         """gg_autotune: the fastest launch shapes for this batch."""
-        t = abi.gg_tuning()
-        _check(lib().gg_autotune(self.system._h, substeps, C.byref(t)))
-        return {k: getattr(t, k) for k, _ in abi.gg_tuning._fields_}
+        return self.system.autotune(substeps)
 
     def capture(self, substeps: int):
         _check(lib().gg_graph_capture(self.system._h, substeps))

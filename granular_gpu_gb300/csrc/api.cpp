@@ -788,8 +788,7 @@ gg_status gg_autotune(gg_system* S, int32_t substeps, gg_tuning* out) {
   GG_GUARD_BEGIN
   REQUIRE(S && substeps > 0, "gg_autotune: bad argument");
   REQUIRE(!S->graph_exec, "gg_autotune: tune before capturing a graph (the graph keeps its launch shapes)");
-  REQUIRE(!((S->phys.is_adaptive == 1 && S->P.merge_enabled) || S->P.target_residual > 0.0f),
-          "gg_autotune: needs a fixed-length substep (no merge/split, no residual mode)");
+  REQUIRE(!(S->P.target_residual > 0.0f), "gg_autotune: not in residual mode (the sweep count varies)");
   GG_CUDA(cudaSetDevice(S->device));
   cudaStream_t st = S->stream;
   GG_CUDA(cudaStreamSynchronize(st));
@@ -812,6 +811,25 @@ gg_status gg_autotune(gg_system* S, int32_t substeps, gg_tuning* out) {
   };
   const int cur0 = S->g.cur, ucur0 = S->u.cur;
   const int64_t steps0 = S->steps, launches0 = S->launches, n_grid0 = S->n_grid;
+  // merge/split moves the particle count and the host-side counters
+  const int64_t n0 = S->n, merged_last0 = S->merged_last, split_last0 = S->split_last;
+  const int64_t merged_total0 = S->merged_total, split_total0 = S->split_total;
+  const int merge_iter0 = S->merge_iter;
+  const int32_t error_word0 = S->error_word;
+  const size_t stats_rows0 = S->stats_rows.size();
+  auto restore_counters = [&]() {
+    S->g.cur = cur0;
+    S->u.cur = ucur0;
+    S->n_grid = n_grid0;
+    S->n = n0;
+    S->merged_last = merged_last0;
+    S->split_last = split_last0;
+    S->merged_total = merged_total0;
+    S->split_total = split_total0;
+    S->merge_iter = merge_iter0;
+    S->error_word = error_word0;
+    S->stats_rows.resize(stats_rows0);
+  };
   const bool timing0 = S->frame_timing;
   S->frame_timing = false;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -822,11 +840,9 @@ gg_status gg_autotune(gg_system* S, int32_t substeps, gg_tuning* out) {
   int trials = 0;
   // device ms of `substeps` substeps after one warm-up substep, from the saved state
   auto trial = [&](float* ms) -> gg_status {
+    restore_counters();
     cudaError_t e = copy_all(false);
     if (e != cudaSuccess) return cuda_status(e, "gg_autotune: restore");
-    S->g.cur = cur0;
-    S->u.cur = ucur0;
-    S->n_grid = n_grid0;
     gg_status r = step_once(S);
     if (r != GG_OK) return r;
     GG_CUDA(cudaEventRecord(e0, st));
@@ -846,7 +862,8 @@ gg_status gg_autotune(gg_system* S, int32_t substeps, gg_tuning* out) {
     std::vector<int> cands;
   };
   Tuning& T = S->tune;
-  std::vector<Site> sites = {{&T.keep_threads, {128, 256}},
+  std::vector<Site> sites = {{&T.sweep_variant, {0, 1}},
+                             {&T.keep_threads, {128, 256}},
                              {&T.build_blocks_per_sm, {4, 8, 16, 32}},
                              {&T.apply_threads, {128, 256}},
                              {&T.predict_threads, {128, 256}},
@@ -869,10 +886,8 @@ gg_status gg_autotune(gg_system* S, int32_t substeps, gg_tuning* out) {
     *site.field = choice;
   }
   // leave the system as it was, with the chosen shapes
+  restore_counters();
   cudaError_t re = copy_all(false);
-  S->g.cur = cur0;
-  S->u.cur = ucur0;
-  S->n_grid = n_grid0;
   S->steps = steps0;
   S->launches = launches0;
   S->frame_timing = timing0;
@@ -887,6 +902,8 @@ gg_status gg_autotune(gg_system* S, int32_t substeps, gg_tuning* out) {
     out->finalize_threads = T.finalize_threads;
     out->keep_threads = T.keep_threads;
     out->build_blocks_per_sm = T.build_blocks_per_sm;
+    out->sweep_variant = T.sweep_variant;
+    out->pad_ = 0;
     out->trials = trials;
     out->ms_default = base;
     out->ms_tuned = best;

@@ -148,6 +148,7 @@ struct Tuning {
   int finalize_threads = 256;
   int keep_threads = 256;
   int build_blocks_per_sm = 16;
+  int sweep_variant = 0;  // variant of the default sweep: 0 contact lists, 1 pruned stencil sweep
 };
 
 struct gg_system {

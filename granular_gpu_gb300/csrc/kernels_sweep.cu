@@ -966,12 +966,13 @@ gg_status sweep(gg_system* S, int it, cudaStream_t st) {
   }
   prof_begin(S, PC_SWEEP, st);
   // reserved[0] selects the sweep variant: 0 (default) contact lists when
-  // they are allocated, else variant 3; 1 one thread per particle with
+  // they are allocated, else variant 3 (or the variant gg_autotune chose); 1 one thread per particle with
   // pruning; 2 shared-memory tile; 3 one thread per particle over all 27
   // cells with a deferred contact list; 4 warp-cooperative with staged
   // candidates; 5 contact lists (variant 3 without them); 6 warp-cooperative
   // over the stencil union
   int variant = S->P.reserved[0];
+  if (variant == 0 && S->tune.sweep_variant != 0) variant = S->tune.sweep_variant;
   if (variant == 0 || variant == 5) variant = S->g.nl_idx ? 5 : 3;
   switch (variant) {
     case 1: {

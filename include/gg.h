@@ -381,13 +381,15 @@ typedef struct gg_tuning {
   int32_t build_blocks_per_sm; /* resident blocks per SM of the list-rebuild sweep */
   int32_t trials;              /* timed trials run */
   float ms_default, ms_tuned;  /* device ms of `substeps` substeps with the shapes before and after */
+  int32_t sweep_variant;       /* default sweep: 0 contact lists, 1 pruned stencil sweep (same bits) */
+  int32_t pad_;
 } gg_tuning;
 /* Times `substeps` substeps for each candidate launch shape of the
- * substep's tunable kernels, one kernel at a time, every trial from the same
- * saved state (restored afterwards: the system is left as it was), and
- * keeps the fastest shapes.  Needs a fixed-length substep (no merge/split,
- * no residual mode); call before gg_graph_capture.  Allocates a device copy
- * of the state while it runs. */
+ * substep's tunable kernels and for the default sweep's variant, one choice
+ * at a time, every trial from the same saved state (restored afterwards: the
+ * system is left as it was, merge/split counters included), and keeps the
+ * fastest.  Not in residual mode; call before gg_graph_capture.  Allocates a
+ * device copy of the state while it runs. */
 gg_status gg_autotune(gg_system* sys, int32_t substeps, gg_tuning* out);
 
 /*

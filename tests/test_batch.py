@@ -87,7 +87,7 @@ def test_autotune_restores_the_state_and_keeps_results():
     a.system.step(4)
     c.system.step(4)
     t = c.autotune(2)
-    assert t["trials"] == 9 and t["ms_tuned"] <= t["ms_default"]  # the default shapes, then 8 others
+    assert t["trials"] == 10 and t["ms_tuned"] <= t["ms_default"]  # the defaults, then 9 other choices
     assert c.system.stats()["steps"] == a.system.stats()["steps"]
     assert np.array_equal(a.system.read(gg.FIELD_POS), c.system.read(gg.FIELD_POS))
     # launch shapes do not change results

@@ -52,3 +52,28 @@ def test_pile_conserves_mass_and_merges():
     m = s.read(gg.FIELD_MASS)
     assert m.max() <= 8.0 and s.size() < desc["n_particles"]
     s.close()
+
+
+def test_autotune_with_merge_split_restores_the_state():
+    # the tuner runs trial substeps (merges and splits included) from a saved
+    # copy and leaves the system as it was; every choice gives the same bits
+    descs = [workloads.adaptive_pile(counts=(24, 24, 24)) for _ in range(2)]
+    a, b = [gg.GranularSystem(**workloads.system_kwargs(d), device=0) for d in descs]
+    a.step(30)
+    b.step(30)
+    st0 = b.stats()
+    t = b.autotune(2)
+    print("pile autotune:", t)
+    assert t["trials"] == 10 and t["sweep_variant"] in (0, 1)
+    st1 = b.stats()
+    for k in ("n_particles", "steps", "merged_total", "split_total", "total_mass_units"):
+        assert st1[k] == st0[k], k
+    assert np.array_equal(a.read(gg.FIELD_POS), b.read(gg.FIELD_POS))
+    for k in range(10):
+        a.step(1)
+        b.step(1)
+        assert a.size() == b.size(), k
+        assert np.array_equal(a.read(gg.FIELD_POS), b.read(gg.FIELD_POS)), k
+    assert np.array_equal(a.read(gg.FIELD_MASS_UNITS), b.read(gg.FIELD_MASS_UNITS))
+    a.close()
+    b.close()
