@@ -149,6 +149,7 @@ class GranularSystem:
         h = C.c_void_p()
         _check(l.gg_create(C.byref(d), C.byref(h)))
         self._h = h
+        self.device = int(device)
         self.cell_size = tuple(int(x) for x in cell_size)
 
     @classmethod
@@ -167,6 +168,7 @@ class GranularSystem:
         h = C.c_void_p()
         _check(lib().gg_create_from_scene(json_path.encode(), C.byref(ov), C.byref(h)))
         self._h = h
+        self.device = int(device)
         cs = (C.c_int32 * 3)()
         _check(lib().gg_grid_dims(h, cs, None))
         self.cell_size = tuple(cs)
@@ -242,6 +244,26 @@ class GranularSystem:
         _check(lib().gg_set_params(self._h, C.byref(p)))
 
     # -- learned warm start -------------------------------------------------
+    def color_buffer(self, mode: int = 2, which: int = SET_GRANULAR, min_mass: float = 1.0,
+                     max_mass: float = 4.0, out=None):
+        """gg_color_buffer: (dots, colors), each an (n, 3) float32 array, as the
+        reference's generate_dots writes them into its vertex buffers.  `out`
+        may give two CUDA tensors of 3 * n floats to fill on the device
+        instead (returned as they are, after the system's stream has run)."""
+        import torch
+        n = self._size(which)
+        if out is None:
+            dots = torch.empty(max(3 * n, 1), dtype=torch.float32, device=f"cuda:{self.device}")
+            cols = torch.empty_like(dots)
+        else:
+            dots, cols = out
+        _check(lib().gg_color_buffer(self._h, which, mode, min_mass, max_mass,
+                                     C.c_void_p(dots.data_ptr()), C.c_void_p(cols.data_ptr())))
+        self.synchronize()
+        if out is not None:
+            return dots, cols
+        return (dots[: 3 * n].view(n, 3).cpu().numpy(), cols[: 3 * n].view(n, 3).cpu().numpy())
+
     def autotune(self, substeps: int = 2) -> dict:
         """gg_autotune: the fastest launch shapes and default-sweep variant
         for this system's current state (the state is left as it was)."""

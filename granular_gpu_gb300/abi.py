@@ -219,6 +219,7 @@ SIGNATURES = {
     "gg_mlp_train_step": (C.c_int, [P_, P_, P_, C.c_int64, C.c_float, C.c_float, C.POINTER(C.c_float), P_]),
     "gg_mlp_destroy": (None, [P_]),
     "gg_selftest_bounded_wait": (C.c_int, [C.c_int32, C.c_int32]),
+    "gg_color_buffer": (C.c_int, [P_, C.c_int, C.c_int32, C.c_float, C.c_float, P_, P_]),
     "gg_set_warm_start": (C.c_int, [P_, P_]),
     "gg_get_params": (C.c_int, [P_, C.POINTER(gg_params)]),
     "gg_set_scenes": (C.c_int, [P_, C.c_int32, C.c_float, C.POINTER(C.c_float)]),

@@ -270,6 +270,18 @@ gg_status gg_read(gg_system* sys, gg_set set, gg_field field,
 gg_status gg_device_ptr(gg_system* sys, gg_set set, gg_field field,
                         void** dptr, int64_t* n, int32_t* stride_bytes);
 
+/* Headless colour buffer: generate_dots (VBO.hpp:9-71, main.cu:1539-1580)
+ * without the OpenGL buffers.  Writes every particle of `set` (GG_SET_GRANULAR
+ * or GG_SET_UPSAMPLED) as a packed float[3] position into d_dots and a packed
+ * float[3] colour into d_colors (device buffers of at least 3 * size floats
+ * each, e.g. a renderer's interop buffers).  mode 0 colours the surface flag,
+ * 1 the surface-distance bands, 2 the mass between min_mass and max_mass (the
+ * reference runs mode 2 with 1 and 4).  Render points have no mass, surface
+ * or distance arrays in the reference beyond zero-filled ones, and are
+ * coloured from zeros.  Enqueued on the system's stream (gg_synchronize). */
+gg_status gg_color_buffer(gg_system* sys, gg_set set, int32_t mode, float min_mass, float max_mass,
+                          float* d_dots, float* d_colors);
+
 /* Overwrites positions/velocities of a set from host float[3] arrays (same
  * count as the set).  Used to start both implementations from one state. */
 gg_status gg_write(gg_system* sys, gg_set set, gg_field field,

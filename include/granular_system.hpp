@@ -72,10 +72,14 @@ class ParticleSetView {
   // (w = radius for positions): a 16-byte stride where the reference has 12.
   float4* get_pos_ptr() const { return (float4*)dptr(GG_FIELD_POS); }
   float4* get_vel_ptr() const { return (float4*)dptr(GG_FIELD_VEL); }
-  float* get_mass_ptr() const { return (float*)dptr(GG_FIELD_MASS); }
-  int* get_surface_ptr() const { return (int*)dptr(GG_FIELD_SURFACE); }
-  float* get_surface_distance_ptr() const { return (float*)dptr(GG_FIELD_SURFACE_DISTANCE); }
+  // Mass, surface and distance exist for the particles only: the render
+  // points' (zero-filled and never written in the reference) read as null.
+  float* get_mass_ptr() const { return (float*)dptr_or_null(GG_FIELD_MASS); }
+  int* get_surface_ptr() const { return (int*)dptr_or_null(GG_FIELD_SURFACE); }
+  float* get_surface_distance_ptr() const { return (float*)dptr_or_null(GG_FIELD_SURFACE_DISTANCE); }
   int* get_particle_2_cell() const { return (int*)dptr(GG_FIELD_CELL_KEY); }
+  gg_system* system() const { return s_; }
+  gg_set set() const { return set_; }
 
  private:
   std::vector<float3> read3(gg_field f) const {
@@ -99,6 +103,12 @@ class ParticleSetView {
     int32_t stride = 0;
     gg_shim::check(gg_device_ptr(s_, set_, f, &p, &n, &stride));
     return p;
+  }
+  void* dptr_or_null(gg_field f) const {
+    void* p = nullptr;
+    int64_t n = 0;
+    int32_t stride = 0;
+    return gg_device_ptr(s_, set_, f, &p, &n, &stride) == GG_OK ? p : nullptr;
   }
   gg_system* s_;
   gg_set set_;
@@ -206,6 +216,14 @@ class GranularSystem {
 
   GranularSolver& get_solver() { return solver_; }
   gg_system* handle() const { return s_; }
+  // GranularSystem.hpp:44-45: the merge limits the colouring uses.
+  float get_max_mass() const { return params().max_mass; }
+  float get_min_mass() const { return params().min_merge_mass; }
+  gg_params params() const {
+    gg_params p;
+    gg_shim::check(gg_get_params(s_, &p));
+    return p;
+  }
 
  private:
   int count(gg_set set) const {
@@ -217,3 +235,18 @@ class GranularSystem {
   GranularSolver solver_;
   std::vector<float> frame_times_;
 };
+
+// generate_dots (VBO.hpp:96-106) over device buffers instead of mapped
+// OpenGL buffer objects: positions and colours of the set as float3, the
+// colour chosen by show_surface (0 surface flag, 1 surface distance, 2 mass
+// between min_mass and max_mass).  The set's own surface array is used, as
+// the reference's callers pass it; `surface` is accepted for the signature.
+// Synchronous, as the reference.
+inline void generate_dots(float3* dot, float3* color, const std::shared_ptr<ParticleSetView>& particles,
+                          int* surface, const float max_mass, const float min_mass, int show_surface) {
+  (void)surface;
+  gg_shim::check(gg_color_buffer(particles->system(), particles->set(), show_surface, min_mass, max_mass,
+                                 reinterpret_cast<float*>(dot), reinterpret_cast<float*>(color)));
+  gg_shim::check(gg_synchronize(particles->system()));
+}
+

@@ -176,3 +176,36 @@ class OracleSystem:
 
 def threads() -> int:
     return int(_fn(lib(False), "threads")())
+
+
+def color_dots(pos, mass=None, surface=None, sdist=None, mode=2, min_mass=1.0, max_mass=4.0):
+    """generate_dots_CUDA (VBO.hpp:9-71) restated in float32 numpy: packed
+    positions and colours.  mode 0: surface == 1 -> (0.34, 0.46, 0.7), else
+    black; mode 1: distance == 0 -> (0.34, 0.46, 0.7), >= 100 -> black, else
+    red; mode 2: (1 - t) * blue + t * red with t = (m - min) / (max - min),
+    and mass == 0 -> (6.0 / 255 / 0, 214 / 255, 160 / 255), first component
+    +inf.  Missing arrays read as the reference's zero-filled ones."""
+    f = np.float32
+    pos = np.asarray(pos, f).reshape(-1, 3)
+    n = pos.shape[0]
+    m = np.zeros(n, f) if mass is None else np.asarray(mass, f)
+    sf = np.zeros(n, np.int32) if surface is None else np.asarray(surface, np.int32)
+    sd = np.zeros(n, f) if sdist is None else np.asarray(sdist, f)
+    col = np.zeros((n, 3), f)
+    blue_grey = np.array([0.34, 0.46, 0.7], f)
+    if mode == 0:
+        col[sf == 1] = blue_grey
+    elif mode == 1:
+        col[sd == 0] = blue_grey
+        col[(sd != 0) & ~(sd >= f(100))] = np.array([1, 0, 0], f)
+    elif mode == 2:
+        with np.errstate(divide="ignore", invalid="ignore", over="ignore"):
+            t = (m - f(min_mass)) / (f(max_mass) - f(min_mass))
+            one_t = f(1) - t
+            # (1 - t) * (0, 0, 1) + t * (1, 0, 0), product then sum per component
+            col[:, 0] = one_t * f(0) + t * f(1)
+            col[:, 1] = one_t * f(0) + t * f(0)
+            col[:, 2] = one_t * f(1) + t * f(0)
+            special = np.array([np.float64(np.inf), 214.0 / 255.0, 160.0 / 255.0]).astype(f)
+        col[m == 0] = special
+    return pos.copy(), col

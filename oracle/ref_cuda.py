@@ -24,7 +24,9 @@ them:
 * `Solver::upsampled_update` (`:1371-1387`) -> `update_upsampled_cuda`;
 * `GranularSystem::set_surface_particles` and `find_distance_to_surface`
   (`src/GranularSystem.cu:613-699`) -> `find_cover_vector`, `find_surface`,
-  `compute_distance_to_surface`.
+  `compute_distance_to_surface`;
+* `generate_dots` (`src/VBO.hpp:96-106`) -> `generate_dots_CUDA`, the colouring
+  of the vertex buffers.
 
 The torch restatements of the functors round as the reference's device code
 does when it is built with `-fmad=false` (the `_nofma` cubins).  With the
@@ -50,12 +52,14 @@ _SIGS = {
     "find_cover_vector": "p p p i p i3 f f",
     "find_surface": "p p p p i p i3 f f",
     "compute_distance_to_surface": "i p p p i3 f p",
+    "generate_dots_CUDA": "p p p i p p f f i p",
 }
 _UNIT_OF = {
     "mapParticles2Cells_CUDA": "solver", "countingInCell_CUDA": "solver",
     "compute_delta_pos": "solver", "update_upsampled_cuda": "solver",
     "find_cover_vector": "gsystem", "find_surface": "gsystem",
     "compute_distance_to_surface": "gsystem",
+    "generate_dots_CUDA": "vbo",
 }
 
 
@@ -115,7 +119,7 @@ class RefKernels:
         suffix = "" if fma else "_nofma"
         self.mods = {}
         self.fns = {}
-        for unit in ("solver", "gsystem"):
+        for unit in ("solver", "gsystem", "vbo"):
             name = f"{unit}{suffix}.cubin"
             mod = C.c_void_p()
             self.d.check(self.d.cu.cuModuleLoad(C.byref(mod), os.path.join(REF_DIR, name).encode()),

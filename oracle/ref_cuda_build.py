@@ -7,12 +7,16 @@ outputs go to `oracle/_ref/` only (git-ignored; they travel to the GPU host
 with the working tree, which has no reference checkout and therefore uses
 the prebuilt files).
 
-  solver.cubin, gsystem.cubin              the reference's own device flags
+  solver.cubin, gsystem.cubin, vbo.cubin   the reference's own device flags
                                            (nvcc defaults: -O3, FMA contraction on)
-  solver_nofma.cubin, gsystem_nofma.cubin  the same with -fmad=false, so every
+  *_nofma.cubin                            the same with -fmad=false, so every
                                            operation rounds as written, as in
                                            this library's build
   entries.json                             {cubin: {kernel name: mangled entry}}
+
+`src/VBO.hpp` (the colouring kernel of the vertex buffers) is a header that
+only `main.cu` includes; it is compiled through a one-line translation unit
+written into `oracle/_ref/` that includes it from the reference checkout.
 
 The entry names are read from `ptxas -v`'s "Compiling entry function" lines.
 The host side of the reference (its thrust calls, its `GranularSystem`
@@ -32,7 +36,7 @@ REF_SRC = os.path.join(os.environ.get("GG_REFERENCE_DIR", "/root/reference"), "s
 CUDA = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA, "bin", "nvcc")
 
-UNITS = {"solver": "Solver.cu", "gsystem": "GranularSystem.cu"}
+UNITS = {"solver": "Solver.cu", "gsystem": "GranularSystem.cu", "vbo": "VBO.hpp"}
 FLAVOURS = {"": [], "_nofma": ["-fmad=false"]}
 ENTRY_RE = re.compile(r"Compiling entry function '(_Z(\d+)([A-Za-z_]\w*?)\w*)' for")
 
@@ -51,11 +55,23 @@ def _kernel_name(mangled: str):
     return mangled[start:start + n]
 
 
-def _compile(unit: str, flavour: str):
+def _source(unit: str) -> str:
+    """The translation unit of `unit`: the reference's .cu file, or for a
+    header a generated file that includes it where it lies."""
     src = os.path.join(REF_SRC, UNITS[unit])
+    if src.endswith(".cu"):
+        return src
+    tu = os.path.join(OUT, f"{unit}_ref.cu")
+    with open(tu, "w") as f:
+        f.write(f'#include "{src}"\n')
+    return tu
+
+
+def _compile(unit: str, flavour: str):
+    src = _source(unit)
     dst = os.path.join(OUT, f"{unit}{flavour}.cubin")
     cmd = [NVCC, "-cubin", "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17",
-           "--extended-lambda", "-w", "-Xptxas", "-v", *FLAVOURS[flavour], src, "-o", dst]
+           "--extended-lambda", "-w", "-Xptxas", "-v", "-I", REF_SRC, *FLAVOURS[flavour], src, "-o", dst]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"reference cubin build failed: {' '.join(cmd)}\n{r.stderr[-4000:]}")

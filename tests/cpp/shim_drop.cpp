@@ -49,6 +49,25 @@ int main(int argc, char** argv) {
     printf("step %d n=%d up=%d walls=%d com_y=%.6f\n", s, sys.size(), sys.upsampled_size(), sys.boundary_size(),
            cy / x.size());
   }
+  // renderUpsampledParticles / renderParticles (main.cu:1539-1580) into device buffers
+  float3 *dd = nullptr, *dc = nullptr;
+  const size_t nu = (size_t)sys.upsampled_size(), n = (size_t)sys.size();
+  if (cudaMalloc(&dd, sizeof(float3) * nu) != cudaSuccess || cudaMalloc(&dc, sizeof(float3) * nu) != cudaSuccess) {
+    fprintf(stderr, "cudaMalloc failed\n");
+    return 3;
+  }
+  generate_dots(dd, dc, sys.get_upsampled(), sys.get_upsampled()->get_surface_ptr(), sys.get_max_mass(),
+                sys.get_min_mass(), 2);
+  std::vector<float3> cu(nu);
+  cudaMemcpy(cu.data(), dc, sizeof(float3) * nu, cudaMemcpyDeviceToHost);
+  generate_dots(dd, dc, sys.get_particles(), sys.get_particles()->get_surface_ptr(), sys.get_max_mass(),
+                sys.get_min_mass(), 2);
+  std::vector<float3> cp(n);
+  cudaMemcpy(cp.data(), dc, sizeof(float3) * n, cudaMemcpyDeviceToHost);
+  cudaFree(dd);
+  cudaFree(dc);
+  // render points have no mass (the reference's 6.0 / 255 / 0 colour); unit masses are blue
+  printf("dots up_inf=%d p0=(%.3f,%.3f,%.3f)\n", (int)(cu[0].x > 1e30f), cp[0].x, cp[0].y, cp[0].z);
   sys.get_solver().save_particle_stats("/tmp/gg_shim_stats.csv");
   printf("frames=%zu\n", sys.get_frame_times().size());
   return 0;

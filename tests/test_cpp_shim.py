@@ -13,7 +13,7 @@ def _build(tmp_path):
     lib_dir = os.path.join(ROOT, "granular_gpu_gb300", "_build")
     cmd = ["g++", "-std=c++17", "-O1", f"-I{ROOT}/include", f"-I{CUDA}/include",
            os.path.join(ROOT, "tests", "cpp", "shim_drop.cpp"), "-o", exe, f"-L{lib_dir}", "-lgg",
-           f"-Wl,-rpath,{lib_dir}"]
+           f"-Wl,-rpath,{lib_dir}", f"-L{CUDA}/lib64", "-lcudart", f"-Wl,-rpath,{CUDA}/lib64"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     return exe
@@ -34,3 +34,4 @@ def test_shim_runs_reference_style_caller(tmp_path):
     ys = [float(l.split("com_y=")[1]) for l in lines]
     assert ys[-1] < ys[0], "the block falls"
     assert "frames=4" in r.stdout  # frame timing starts after the constructor's step
+    assert "dots up_inf=1 p0=(0.000,0.000,1.000)" in r.stdout, r.stdout

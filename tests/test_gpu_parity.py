@@ -385,3 +385,21 @@ def test_host_copies_pinned_misaligned_and_pageable_agree():
         s.write(gg.FIELD_POS, buf)
         assert np.array_equal(s.read(gg.FIELD_POS), moved)
     s.close()
+
+
+@pytest.mark.parametrize("mode", [0, 1, 2])
+def test_color_buffer_matches_oracle(mode):
+    desc = workloads.box_drop(n_side=12, substeps=4, iters=5, adaptive=1, upsample_per=2)
+    s = gg.GranularSystem(**workloads.system_kwargs(desc), device=0)
+    s.step(45)
+    for which in (gg.SET_GRANULAR, gg.SET_UPSAMPLED):
+        dots, cols = s.color_buffer(mode, which, 1.0, 4.0)
+        if which == gg.SET_GRANULAR:
+            od, oc = orc.color_dots(s.read(gg.FIELD_POS), s.read(gg.FIELD_MASS), s.read(gg.FIELD_SURFACE),
+                                    s.read(gg.FIELD_SURFACE_DISTANCE), mode, 1.0, 4.0)
+        else:
+            od, oc = orc.color_dots(s.read(gg.FIELD_POS, gg.SET_UPSAMPLED), mode=mode)
+        assert np.array_equal(dots, od) and np.array_equal(cols, oc), which
+    with pytest.raises(gg.GranularError):
+        s.color_buffer(3)
+    s.close()

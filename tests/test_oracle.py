@@ -133,3 +133,16 @@ def test_particle_stats_csv(tmp_path):
     lines = path.read_text().strip().splitlines()
     assert lines[0] == "Frame,MergedParticles,SplitParticles,TotalParticles"
     assert len(lines) == 1 + 3  # constructor step + 2 steps
+
+
+def test_color_dots_known_answers():
+    # generate_dots_CUDA (VBO.hpp:9-71) read as written
+    p = np.arange(12, dtype=np.float32).reshape(4, 3)
+    d, c = orc.color_dots(p, mass=[0, 1, 2.5, 4], mode=2)
+    assert np.array_equal(d, p)
+    assert np.isinf(c[0, 0]) and c[0, 1] == np.float32(214 / 255) and c[0, 2] == np.float32(160 / 255)
+    assert np.array_equal(c[1:], np.array([[0, 0, 1], [0.5, 0, 0.5], [1, 0, 0]], np.float32))
+    _, c = orc.color_dots(p, surface=[0, 1, 2, 1], mode=0)
+    assert np.array_equal(c[:, 0], np.array([0, 0.34, 0, 0.34], np.float32))
+    _, c = orc.color_dots(p, sdist=[0, 5, 100, np.nan], mode=1)
+    assert np.array_equal(c, np.array([[0.34, 0.46, 0.7], [1, 0, 0], [0, 0, 0], [1, 0, 0]], np.float32))

@@ -360,3 +360,36 @@ def test_throughput_against_reference_kernels(kernels, counts):
           f"{ms_ref:.1f} ms per substep, this library {ms_ours:.2f} ms: {ms_ref / ms_ours:.1f}x")
     assert ms_ref / ms_ours >= 1.5
     s.close()
+
+
+@pytest.mark.parametrize("mode", [0, 1, 2])
+def test_color_buffer_matches_reference_kernel(kernels, mode):
+    # generate_dots_CUDA (VBO.hpp) on the same state: particles after merges
+    # have started (blended masses, surface flags and distances), render
+    # points with the reference's zero-filled mass, surface and distance
+    import torch
+    desc = _box(n_side=12, upsample_per=2, adaptive=1)
+    s = gg.GranularSystem(**workloads.system_kwargs(desc), device=0)
+    s.step(45)
+    masses = s.read(gg.FIELD_MASS)
+    assert (masses != 1.0).any()
+    for which in (gg.SET_GRANULAR, gg.SET_UPSAMPLED):
+        dots, cols = s.color_buffer(mode, which, 1.0, 4.0)
+        n = dots.shape[0]
+        pos = _t(s.read(gg.FIELD_POS, which))
+        if which == gg.SET_GRANULAR:
+            mass, surf = _t(masses), _t(s.read(gg.FIELD_SURFACE).astype(np.int32))
+            sd = _t(s.read(gg.FIELD_SURFACE_DISTANCE))
+        else:
+            mass, sd = torch.zeros(n, device="cuda"), torch.zeros(n, device="cuda")
+            surf = torch.zeros(n, dtype=torch.int32, device="cuda")
+        for fma in (False, True):
+            rd = torch.empty((n, 3), dtype=torch.float32, device="cuda")
+            rc = torch.empty_like(rd)
+            kernels[fma].launch("generate_dots_CUDA", n, rd, rc, pos, n, surf, mass, 4.0, 1.0, mode, sd)
+            kernels[fma].synchronize()
+            assert _ndiff(dots, rd.cpu().numpy()) == 0, (which, fma)
+            assert _ndiff(cols, rc.cpu().numpy()) == 0, (which, fma)
+        if mode == 2 and which == gg.SET_UPSAMPLED:
+            assert np.isinf(cols[:, 0]).all()  # mass 0: the reference's 6.0 / 255 / 0
+    s.close()
