@@ -290,6 +290,32 @@ class GranularSystem:
         """ASCII VTK point cloud (the reference's writers, main.cu:190-254)."""
         _check(lib().gg_write_vtk(self._h, which, path.encode(), int(bool(swap_yz))))
 
+    def write_vtk_centered(self, path: str, which: int = SET_UPSAMPLED):
+        """saveUpsampledPositionsToVTK (main.cu:588-664)."""
+        _check(lib().gg_write_vtk_centered(self._h, which, path.encode()))
+
+    def write_vtk_by_mass(self, base: str, frame_id: int):
+        """saveParticlesByMass (main.cu:256-368)."""
+        _check(lib().gg_write_vtk_by_mass(self._h, base.encode(), int(frame_id)))
+
+    def write_vtk_animated_boundary(self, path: str, centred: bool = True):
+        """saveBoundaryParticlesToVTK / saveFunnelBoundaryParticlesToVTK
+        (main.cu:434-527 / 370-432)."""
+        _check(lib().gg_write_vtk_animated_boundary(self._h, path.encode(), int(bool(centred))))
+
+    def write_vtk_points_centered(self, points, path: str):
+        """saveAdditionalBoundaryParticlesToVTK (main.cu:529-586)."""
+        a = _f32(points)
+        _check(lib().gg_write_vtk_points_centered(self._h, a.ctypes.data_as(C.c_void_p), a.shape[0], path.encode()))
+
+    def write_csv(self, path: str, which: int = SET_UPSAMPLED):
+        """saveUpsampledPositionsToCSV (main.cu:673-694)."""
+        _check(lib().gg_write_csv(self._h, which, path.encode()))
+
+    def write_frame_times(self, path: str):
+        """saveFrameTimes (main.cu:665-671)."""
+        _check(lib().gg_write_frame_times(self._h, path.encode()))
+
     def save(self, path: str):
         _check(lib().gg_save(self._h, path.encode()))
 

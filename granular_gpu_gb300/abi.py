@@ -220,6 +220,12 @@ SIGNATURES = {
     "gg_mlp_destroy": (None, [P_]),
     "gg_selftest_bounded_wait": (C.c_int, [C.c_int32, C.c_int32]),
     "gg_color_buffer": (C.c_int, [P_, C.c_int, C.c_int32, C.c_float, C.c_float, P_, P_]),
+    "gg_write_vtk_centered": (C.c_int, [P_, C.c_int, C.c_char_p]),
+    "gg_write_vtk_by_mass": (C.c_int, [P_, C.c_char_p, C.c_int32]),
+    "gg_write_vtk_animated_boundary": (C.c_int, [P_, C.c_char_p, C.c_int32]),
+    "gg_write_vtk_points_centered": (C.c_int, [P_, P_, C.c_int64, C.c_char_p]),
+    "gg_write_csv": (C.c_int, [P_, C.c_int, C.c_char_p]),
+    "gg_write_frame_times": (C.c_int, [P_, C.c_char_p]),
     "gg_set_warm_start": (C.c_int, [P_, P_]),
     "gg_get_params": (C.c_int, [P_, C.POINTER(gg_params)]),
     "gg_set_scenes": (C.c_int, [P_, C.c_int32, C.c_float, C.POINTER(C.c_float)]),

@@ -302,6 +302,30 @@ gg_status gg_save_particle_stats(gg_system* sys, const char* path);
  * positions are dropped and, with swap_yz, points are written "x z y". */
 gg_status gg_write_vtk(gg_system* sys, gg_set set, const char* path, int32_t swap_yz);
 
+/* The reference's other frame writers (main.cu:256-694), ASCII VTK point
+ * clouds written "x z y" like gg_write_vtk:
+ *   gg_write_vtk_centered           saveUpsampledPositionsToVTK (:588-664): the
+ *                                   set's valid points centred on their centroid,
+ *                                   the lowest lifted to y = 0;
+ *   gg_write_vtk_by_mass            saveParticlesByMass (:256-368): the particles,
+ *                                   centred, into <base>_mass_light|_medium|_heavy/
+ *                                   <frame_id>.vtk (mass < 2, 2..3, above);
+ *   gg_write_vtk_animated_boundary  saveFunnelBoundaryParticlesToVTK (:370-432,
+ *                                   centred = 0) / saveBoundaryParticlesToVTK
+ *                                   (:434-527, centred on the render points);
+ *   gg_write_vtk_points_centered    saveAdditionalBoundaryParticlesToVTK
+ *                                   (:529-586): caller points (float[3]), centred
+ *                                   on the render points;
+ *   gg_write_csv                    saveUpsampledPositionsToCSV (:673-694): "x,y,z";
+ *   gg_write_frame_times            saveFrameTimes (:665-671).
+ * Writers that find nothing to write leave an empty file, as the reference's. */
+gg_status gg_write_vtk_centered(gg_system* sys, gg_set set, const char* path);
+gg_status gg_write_vtk_by_mass(gg_system* sys, const char* base, int32_t frame_id);
+gg_status gg_write_vtk_animated_boundary(gg_system* sys, const char* path, int32_t centred);
+gg_status gg_write_vtk_points_centered(gg_system* sys, const float* points3, int64_t n, const char* path);
+gg_status gg_write_csv(gg_system* sys, gg_set set, const char* path);
+gg_status gg_write_frame_times(gg_system* sys, const char* path);
+
 /* GranularSystem::get_frame_times (GranularSystem.hpp:48): per-step device
  * milliseconds, recorded when timing is enabled. */
 gg_status gg_set_frame_timing(gg_system* sys, int32_t enabled);
