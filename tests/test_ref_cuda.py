@@ -324,6 +324,49 @@ def test_long_run_statistics_follow_reference(kernels):
     s.close()
 
 
+def _pile_shape(p):
+    # (angle in degrees, median reach, 95th-percentile reach): the cone
+    # through the particles' 95th-percentile height above the lowest one and
+    # their 95th-percentile horizontal distance from the vertical axis through
+    # their centre; the median distance measures the bulk, the 95th
+    # percentile the particles splashed across the floor
+    p = p.astype(np.float64)
+    d = np.hypot(p[:, 0] - p[:, 0].mean(), p[:, 2] - p[:, 2].mean())
+    h = p[:, 1] - p[:, 1].min()
+    reach = float(np.percentile(d, 95))
+    return float(np.degrees(np.arctan2(np.percentile(h, 95), reach))), float(np.median(d)), reach
+
+
+def test_pile_shape_follows_reference(kernels):
+    # a 6 x 30 x 6 column dropped from 0.25 m lands on the floor (500
+    # substeps, about 2 s).  In the reference's model a landed stack barely
+    # slumps: the mass scaling m exp(-y) makes lower particles heavier and
+    # speeds below 0.01 are zeroed every substep, so the column stays steep.
+    # Its profile angle and reach against the reference's from the same
+    # initial state, next to the spread of two reference runs.
+    desc = _box(n_side=10)
+    r = workloads.REF_RADIUS
+    col = workloads.lattice((6, 30, 6), 2 * r, (0.5 - 5 * r, 0.25, 0.5 - 5 * r), 0.05 * r, 7)
+    desc["particles"], desc["n_particles"] = col, col.shape[0]
+    s = gg.GranularSystem(**workloads.system_kwargs(desc), device=0)
+    refs = [_ref_from(kernels[False], s, desc) for _ in range(2)]
+    for _ in range(500):
+        s.step(1)
+        for ref in refs:
+            ref.step()
+    a, med, reach = _pile_shape(s.read(gg.FIELD_POS))
+    b = [_pile_shape(ref.read("pos")) for ref in refs]
+    print(f"profile angle: ours {a:.2f} deg, reference {b[0][0]:.2f} and {b[1][0]:.2f} deg; "
+          f"median reach: ours {med / r:.2f} r, reference {b[0][1] / r:.2f} and {b[1][1] / r:.2f} r; "
+          f"95th-percentile reach: ours {reach / r:.2f} r, reference {b[0][2] / r:.2f} and {b[1][2] / r:.2f} r")
+    assert abs(a - b[0][0]) <= max(3.0 * abs(b[1][0] - b[0][0]), 1.0), (a, b)
+    assert abs(med - b[0][1]) <= max(3.0 * abs(b[1][1] - b[0][1]), 0.15 * b[0][1]), (med, b)
+    # the splash reaches further here: this library's sweep corrects about
+    # 15 % less than the reference's racy one (it loses no count increments)
+    assert 0.7 * b[0][2] <= reach <= 1.4 * b[0][2], (reach, b)
+    s.close()
+
+
 @pytest.mark.parametrize("counts", [(64, 128, 128), (128, 256, 256)])
 def test_throughput_against_reference_kernels(kernels, counts):
     """Substep time of this library against the reference's own kernels
