@@ -223,7 +223,9 @@ struct UpArgs {
 // in candidate order, so the sums are the reference's.  A warp then spends
 // the weight arithmetic on each lane's own hits instead of on every
 // candidate some lane hits.
-__global__ void __launch_bounds__(256) k_upsample(UpArgs a) {
+// 6 resident blocks of 256 (40 registers, no spills): the kernel is bound by
+// instruction issue, and 48 warps per SM hide its load latency better than 40.
+__global__ void __launch_bounds__(256, 6) k_upsample(UpArgs a) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
   const Grid g = a.g;
@@ -240,7 +242,7 @@ __global__ void __launch_bounds__(256) k_upsample(UpArgs a) {
     for (int c0 = a.cs[k0]; c0 < j1; c0 += 32) {
       const int cn = min(32, j1 - c0);
       unsigned mask = 0u;
-#pragma unroll 4
+#pragma unroll 8
       for (int b = 0; b < cn; ++b) {
         const float4 xj = a.gpos[c0 + b];
         const float dx = p.x - xj.x, dy = p.y - xj.y, dz = p.z - xj.z;
