@@ -56,7 +56,8 @@ __constant__ int kTowards[9][2] = {{1, 1}, {1, 0}, {0, 1}, {0, 0}, {1, -1}, {-1,
 template <int MM>
 __global__ void __launch_bounds__(256) k_surface(Grid g, int n, const float4* __restrict__ pos,
                                                  const float* __restrict__ rs, const int32_t* __restrict__ cs,
-                                                 int32_t* __restrict__ surface, float cone, int min_nb) {
+                                                 int32_t* __restrict__ surface, float cone, float cos_cone,
+                                                 int min_nb) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const float3 xi = f3(pos[i]);
@@ -91,8 +92,8 @@ __global__ void __launch_bounds__(256) k_surface(Grid g, int n, const float4* __
   // the end c.z points to, so that an interior particle meets a neighbour
   // inside the cone early.  acos(d) <= cone is decided from d alone away
   // from cos(cone) (the margin of 1e-5 on d is some 40 times the bound on
-  // acosf's error there); near it acos is evaluated.
-  const float cos_cone = cosf(cone);
+  // acosf's error there and over the rounding of cos_cone, computed on the
+  // host); near it acos is evaluated.
   const float d_in = cos_cone + 1e-5f, d_out = cos_cone - 1e-5f;
   const int sx = c.x < 0.0f ? -1 : 1, sy = c.y < 0.0f ? -1 : 1;
   const bool up = c.z > 0.0f;
@@ -184,10 +185,16 @@ gg_status surface(gg_system* S, cudaStream_t st) {
   if (S->n <= 0) return GG_OK;
   const int c = S->g.cur;
   prof_begin(S, PC_SURFACE, st);
-  auto kern = S->P.reserved[1] != 1 ? (S->P.math_mode ? k_surface<1> : k_surface<0>)
-                                    : (S->P.math_mode ? k_surface_warp<1> : k_surface_warp<0>);
-  kern<<<blocks_for(S->n, 256), 256, 0, st>>>(S->grid, (int)S->n, S->g.pos[c], S->g.rs[c], S->g.cell_start,
-                                                   S->g.surface, S->P.surface_cone, S->P.surface_min_neighbors);
+  if (S->P.reserved[1] != 1) {
+    auto kern = S->P.math_mode ? k_surface<1> : k_surface<0>;
+    kern<<<blocks_for(S->n, 256), 256, 0, st>>>(S->grid, (int)S->n, S->g.pos[c], S->g.rs[c], S->g.cell_start,
+                                                 S->g.surface, S->P.surface_cone, std::cos(S->P.surface_cone),
+                                                 S->P.surface_min_neighbors);
+  } else {
+    auto kern = S->P.math_mode ? k_surface_warp<1> : k_surface_warp<0>;
+    kern<<<blocks_for(S->n, 256), 256, 0, st>>>(S->grid, (int)S->n, S->g.pos[c], S->g.rs[c], S->g.cell_start,
+                                                 S->g.surface, S->P.surface_cone, S->P.surface_min_neighbors);
+  }
   count_launches(S, 1);
   prof_end(S, PC_SURFACE, S->n, st);
   GG_CUDA(cudaGetLastError());
