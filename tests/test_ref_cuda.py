@@ -372,7 +372,7 @@ def test_throughput_against_reference_kernels(kernels, counts):
     """Substep time of this library against the reference's own kernels
     (own flags, driven by the harness's host restatement) on the column
     collapse without merge/split, upsampling on, the reference's constants
-    as compiled in: the benchmark spec asks for at least 1.5x."""
+    as compiled in: this library must be at least 1.5x as fast."""
     import torch
     desc = workloads.column_collapse(counts=counts, adaptive=0, upsample_per=4)
     p = workloads.scaled_params(workloads.REF_RADIUS, iters=5)
