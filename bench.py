@@ -331,6 +331,10 @@ def run_mine(args):
                      "algorithmic_bytes_per_unit": per_unit, "unit_of_work": unit_name,
                      "bytes_basis": byte_note, "units_per_launch": units_per_launch,
                      "avg_launch_ms": avg_ms, "shares": shares,
+                     # the same ncu capture's issue figures: the stencil kernels are
+                     # bound by instruction issue, not by HBM
+                     "issue_active_pct": (tr or {}).get("issue_active_pct"),
+                     "sm_throughput_pct": (tr or {}).get("sm_throughput_pct"),
                      "list_builds_per_particle_sweep": list_builds / max(prof["sweep"]["units"], 1)},
         "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d // max(args.steps, 1),
                 "d2h_bytes_per_step": d2h // max(args.steps, 1)},
