@@ -83,7 +83,7 @@ __device__ __forceinline__ unsigned axis_mask(float x, int q, float L, float R) 
 struct Target {
   float3 x;
   float rc, rb;
-  double Bd;      // 0.01 + r_b in double (Solver.cu:283)
+  float Bf;       // 0.01 + r_b in double (Solver.cu:283), rounded to float
   float Bru;      // Bd rounded up to float: (double)d < Bd  <=>  d < Bru for every float d
   float capBru;   // (r_b + 0.01) * 0.8 in double, rounded up to float (same use)
   float Bcut;     // conservative float cut for the wall test
@@ -92,8 +92,18 @@ struct Target {
   bool binned;
   int cx, cy, cz; // binning cell
   unsigned pm[3], bm[3];
-  double fcap;    // friction cap factor (0.8 in the reference; per scene in a batch)
+  float fcapf;    // friction cap factor (0.8 in the reference; per scene in a batch), as float
 };
+
+// The friction cap in double, as the reference's comparisons and ratios use
+// it (rare paths only, so targets carry the float copy).
+__device__ __forceinline__ double target_fcap(const SweepArgs& a, const Target& t) {
+  if (!a.scene_fcap) return a.fcap;
+  const int s = min(max(__float2int_rz(t.x.x * a.scene_inv_w), 0), a.n_scenes - 1);
+  return (double)a.scene_fcap[s];
+}
+// 0.01 + r_b in double (Solver.cu:283).
+__device__ __forceinline__ double target_bd(const SweepArgs& a, const Target& t) { return a.brad + (double)t.rb; }
 
 // The per-target values every sweep needs (no pruning masks).
 __device__ __forceinline__ void make_target_lite(const SweepArgs& a, int i, float4 xi4, Target& t) {
@@ -101,16 +111,13 @@ __device__ __forceinline__ void make_target_lite(const SweepArgs& a, int i, floa
   t.x = f3(xi4);
   t.rc = xi4.w;
   t.rb = fmaxf(t.rc, a.minr);
-  t.Bd = a.brad + (double)t.rb;
-  t.Bru = __double2float_ru(t.Bd);
-  t.fcap = a.fcap;
-  if (a.scene_fcap) {
-    const int s = min(max(__float2int_rz(t.x.x * a.scene_inv_w), 0), a.n_scenes - 1);
-    t.fcap = (double)a.scene_fcap[s];
-  }
-  t.capBru = __double2float_ru(((double)t.rb + a.brad) * t.fcap);
-  const float Bf = (float)t.Bd;
-  t.Bcut = Bf * Bf * 1.0001f;
+  const double Bd = target_bd(a, t);
+  t.Bru = __double2float_ru(Bd);
+  const double fcap = target_fcap(a, t);
+  t.fcapf = (float)fcap;
+  t.capBru = __double2float_ru(((double)t.rb + a.brad) * fcap);
+  t.Bf = (float)Bd;
+  t.Bcut = t.Bf * t.Bf * 1.0001f;
   t.inv_m = a.inv_m[i];
   t.q = trunc_cell(g, t.x);
   const uint32_t key = a.keys[i];
@@ -135,7 +142,7 @@ __device__ __forceinline__ void target_masks(const SweepArgs& a, Target& t) {
   const float ax = fmaxf(fmaxf(fabsf(t.x.x), fabsf(t.x.y)), fabsf(t.x.z));
   const float slack = 4e-6f * (ax + 1.0f) + 1e-5f * g.L;
   const float Rp = (t.rc + rmax + disp) * 1.0001f + slack;
-  const float Rb = (float)t.Bd * 1.0001f + slack;
+  const float Rb = t.Bf * 1.0001f + slack;
   t.pm[0] = axis_mask(t.x.x, t.q.x, g.L, Rp);
   t.pm[1] = axis_mask(t.x.y, t.q.y, g.L, Rp);
   t.pm[2] = axis_mask(t.x.z, t.q.z, g.L, Rp);
@@ -158,7 +165,7 @@ __device__ __forceinline__ void wall_contact(const SweepArgs& a, const Target& t
   const float bx = t.x.x - pb.x, by = t.x.y - pb.y, bz = t.x.z - pb.z;
   const float dis = m_norm3<MM>(bx, by, bz);
   if (!(dis < t.Bru)) return;  // mag < 0
-  const float mag = (float)((double)dis - t.Bd);
+  const float mag = (float)((double)dis - target_bd(a, t));
   const float3 p12 = make_float3(bx, by, bz);
   const float3 dpi = smul3(mag / dis, p12);
   const float3 perp = sub3(dpi, div3s(smul3(dot3(dpi, p12), p12), dis * dis));
@@ -166,7 +173,7 @@ __device__ __forceinline__ void wall_contact(const SweepArgs& a, const Target& t
   if (pn < t.capBru) {
     dp = sub3(dp, dpi);
   } else {
-    const float minf = (float)fmin((a.brad + (double)t.rb) * t.fcap / (double)pn, 1.0);
+    const float minf = (float)fmin((a.brad + (double)t.rb) * target_fcap(a, t) / (double)pn, 1.0);
     dp = sub3(dp, mul3s(dpi, minf));
   }
   ++c;
@@ -209,7 +216,7 @@ __device__ __forceinline__ void particle_pair_f(const SweepArgs& a, const Target
   const float3 dpj = smul3((inv_sum * inv_mj) * tt, p12);
   const float3 dpij = sub3(dpi, dpj);
   const float w = inv_sum * t.inv_m;
-  const float capf = rr * (float)t.fcap;
+  const float capf = rr * t.fcapf;
   // The tangential part `perp` of dpij (which is parallel to p12) is
   // rounding noise: |perp| <= 2 (|a| + |b|) dis (1 + 8 eps) with a, b the
   // two scalar factors above.  When that bound is below the cap the
@@ -225,12 +232,12 @@ __device__ __forceinline__ void particle_pair_f(const SweepArgs& a, const Target
     // (double)pn < (double)rr * 0.8, decided in float when clear-cut
     if (pn < capf * 0.999999f) within = true;
     else if (pn > capf * 1.000001f) within = false;
-    else within = (double)pn < (double)rr * t.fcap;
+    else within = (double)pn < (double)rr * target_fcap(a, t);
   }
   if (within) {
     dp = sub3(dp, smul3(w, dpij));
   } else {
-    const float minf = (float)fmin((double)rr * t.fcap / (double)pn, 1.0);
+    const float minf = (float)fmin((double)rr * target_fcap(a, t) / (double)pn, 1.0);
     dp = sub3(dp, mul3s(smul3(w, dpij), minf));
   }
   ++c;
@@ -804,7 +811,9 @@ __device__ __forceinline__ float nlist_cell_bound(const SweepArgs& a, int3 q, ui
 // Sweeps after the first: particles whose list is still exact run it; the
 // others are queued for k_sweep_nlist_build.
 template <int MM>
-__global__ void __launch_bounds__(256, 4) k_sweep_nlist_keep(SweepArgs a) {
+// 5 resident blocks of 256 (48 registers; the per-target state carries no
+// double, and a few bytes spill): about 2 % faster than 4 blocks at 64.
+__global__ void __launch_bounds__(256, 5) k_sweep_nlist_keep(SweepArgs a) {
   const Grid& g = a.g;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   bool rebuild = false;
@@ -870,7 +879,7 @@ __global__ void __launch_bounds__(kBuildThreads, 8) k_sweep_nlist_build(SweepArg
     const int i = queued ? a.nl_queue[slot] : slot;
     Target t;
     make_target_lite(a, i, a.xs[i], t);
-    const float Bs = (float)t.Bd + a.skin;
+    const float Bs = t.Bf + a.skin;
     const float Bs2 = Bs * Bs * 1.0001f;
     const float rcs = t.rc + a.skin;
     int cnt = 0;
