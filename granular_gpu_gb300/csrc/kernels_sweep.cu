@@ -887,8 +887,11 @@ __global__ void __launch_bounds__(kBuildThreads, 8) k_sweep_nlist_build(SweepArg
       if (cnt < kNlistMax) s_list[w][cnt][lane] = e;
       ++cnt;
     };
-    // candidates in chunks of 32: a mask of those within reach, then the
-    // pushes in index order
+    // candidates in chunks of 32: a mask of those within the reach of the
+    // largest contact radius of the substep, then, in index order, the
+    // exact reach test for each and the pushes
+    const float rmax = __uint_as_float(a.scal->rmax_bits);
+    const float wide = (rcs + rmax) * (rcs + rmax) * 1.0001f;
     auto scan_particles = [&](int j0, int j1) {
       for (int c0 = j0; c0 < j1; c0 += 32) {
         const int cn = min(32, j1 - c0);
@@ -897,15 +900,19 @@ __global__ void __launch_bounds__(kBuildThreads, 8) k_sweep_nlist_build(SweepArg
         for (int b = 0; b < cn; ++b) {
           const float4 xj = a.xs[c0 + b];
           const float dx = t.x.x - xj.x, dy = t.x.y - xj.y, dz = t.x.z - xj.z;
-          const float rs = rcs + xj.w;
           const float d2 = __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmul_rn(dz, dz)));
-          mask |= (d2 > rs * rs * 1.0001f ? 0u : 1u) << b;
+          mask |= (d2 > wide ? 0u : 1u) << b;
         }
         const unsigned self = (unsigned)(i - c0);
         if (self < 32u) mask &= ~(1u << self);
         while (mask) {
-          push(c0 + __ffs(mask) - 1);
+          const int j = c0 + __ffs(mask) - 1;
           mask &= mask - 1u;
+          const float4 xj = a.xs[j];
+          const float dx = t.x.x - xj.x, dy = t.x.y - xj.y, dz = t.x.z - xj.z;
+          const float rs = rcs + xj.w;
+          const float d2 = __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmul_rn(dz, dz)));
+          if (!(d2 > rs * rs * 1.0001f)) push(j);
         }
       }
     };
