@@ -16,33 +16,20 @@ namespace gg {
 // ------------------------------------------------------------ surface
 
 // Prefilter of the neighbour test |d| <= 2 (r_i + r_j) with the surface-law
-// radius r_j: the contact radius in pos.w is never smaller (it divides by
-// the density truncated to an integer), so a candidate beyond
-// 2 (r_i + w_j), with a margin far above the roundings of a fused dot
-// product, fails the exact test; it is skipped without loading r_j.
-__device__ __forceinline__ bool far_for_surface(float3 d, float ri, float wj) {
-  const float dd = __fmaf_rn(d.x, d.x, __fmaf_rn(d.y, d.y, __fmul_rn(d.z, d.z)));
-  const float R = 2.0002f * (ri + wj);
-  return dd > R * R;
-}
-
-// find_cover_vector + find_surface (GranularSystem.cu:506-611) fused: the
-// cover vector of i is only needed by i, so one thread makes both passes.
-// The second pass of the reference counts the neighbours within
-// 2 (r_i + r_j) (the same set the first pass sums over, with the same
-// distance test) and ORs a cone vote over them; the flag only depends on
-// (count <= 5 || !vote).  So the count comes from the first pass, a count
-// of at most 5 decides the flag without a second pass, and the second pass
-// stops at the first vote: the flags are the reference's.
-// Marks, in bit b, the candidates c0 + b (b < cn <= 32) that pass the
-// surface-law prefilter, leaving out i itself.
+// radius r_j: no contact radius (pos.w, which divides by the density
+// truncated to an integer) is below the surface-law radius, so with the
+// substep's largest contact radius w_max, a candidate beyond
+// R = 2.0002 (r_i + w_max), with a margin far above the roundings of a fused
+// dot product, fails the exact test.  Marks, in bit b, the candidates
+// c0 + b (b < cn <= 32) within R (R2 = R * R), leaving out i itself.
 __device__ __forceinline__ unsigned surface_chunk_mask(const float4* __restrict__ pos, int c0, int cn, int i,
-                                                       float3 xi, float ri) {
+                                                       float3 xi, float R2) {
   unsigned mask = 0u;
 #pragma unroll 4
   for (int b = 0; b < cn; ++b) {
-    const float4 xj = pos[c0 + b];
-    mask |= (far_for_surface(sub3(xi, f3(xj)), ri, xj.w) ? 0u : 1u) << b;
+    const float3 d = sub3(xi, f3(pos[c0 + b]));
+    const float dd = __fmaf_rn(d.x, d.x, __fmaf_rn(d.y, d.y, __fmul_rn(d.z, d.z)));
+    mask |= (dd > R2 ? 0u : 1u) << b;
   }
   const unsigned self = (unsigned)(i - c0);
   if (self < 32u) mask &= ~(1u << self);
@@ -57,12 +44,14 @@ template <int MM>
 __global__ void __launch_bounds__(256) k_surface(Grid g, int n, const float4* __restrict__ pos,
                                                  const float* __restrict__ rs, const int32_t* __restrict__ cs,
                                                  int32_t* __restrict__ surface, float cone, float cos_cone,
-                                                 int min_nb) {
+                                                 int min_nb, const unsigned int* __restrict__ rmax_bits) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const float3 xi = f3(pos[i]);
   const int3 q = trunc_cell(g, xi);
   const float ri = rs[i];
+  const float Rw = 2.0002f * (ri + __uint_as_float(*rmax_bits));
+  const float R2 = Rw * Rw;
   float3 cv = make_float3(0.f, 0.f, 0.f);
   unsigned nn = 0;
   // Each stencil column is scanned in chunks of 32: the prefilter marks
@@ -71,7 +60,7 @@ __global__ void __launch_bounds__(256) k_surface(Grid g, int n, const float4* __
   for_each_stencil_column(g, q, [&](int k0, int nc) {
     const int j1 = cs[k0 + nc];
     for (int c0 = cs[k0]; c0 < j1; c0 += 32) {
-      unsigned mask = surface_chunk_mask(pos, c0, min(32, j1 - c0), i, xi, ri);
+      unsigned mask = surface_chunk_mask(pos, c0, min(32, j1 - c0), i, xi, R2);
       while (mask) {
         const int j = c0 + __ffs(mask) - 1;
         mask &= mask - 1u;
@@ -109,7 +98,7 @@ __global__ void __launch_bounds__(256) k_surface(Grid g, int n, const float4* __
       const int nch = (j1 - j0 + 31) >> 5;
       for (int ch = 0; ch < nch && !vote; ++ch) {
         const int c0 = j0 + 32 * (up ? nch - 1 - ch : ch);
-        unsigned mask = surface_chunk_mask(pos, c0, min(32, j1 - c0), i, xi, ri);
+        unsigned mask = surface_chunk_mask(pos, c0, min(32, j1 - c0), i, xi, R2);
         while (mask) {
           const int bit = up ? 31 - __clz(mask) : __ffs(mask) - 1;
           mask &= ~(1u << bit);
@@ -189,7 +178,7 @@ gg_status surface(gg_system* S, cudaStream_t st) {
     auto kern = S->P.math_mode ? k_surface<1> : k_surface<0>;
     kern<<<blocks_for(S->n, 256), 256, 0, st>>>(S->grid, (int)S->n, S->g.pos[c], S->g.rs[c], S->g.cell_start,
                                                  S->g.surface, S->P.surface_cone, std::cos(S->P.surface_cone),
-                                                 S->P.surface_min_neighbors);
+                                                 S->P.surface_min_neighbors, &S->scal->rmax_bits);
   } else {
     auto kern = S->P.math_mode ? k_surface_warp<1> : k_surface_warp<0>;
     kern<<<blocks_for(S->n, 256), 256, 0, st>>>(S->grid, (int)S->n, S->g.pos[c], S->g.rs[c], S->g.cell_start,
