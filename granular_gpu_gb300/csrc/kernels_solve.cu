@@ -83,7 +83,7 @@ __global__ void __launch_bounds__(256) k_apply(int n, float4* __restrict__ xs, f
                         const float4* __restrict__ delta, int32_t* __restrict__ s_extra,
                         int32_t* __restrict__ ncon, int32_t* __restrict__ contacts, int stab, int last,
                         unsigned int* __restrict__ inc_bits, const uint32_t* __restrict__ keys,
-                        uint32_t* __restrict__ cell_inc) {
+                        uint32_t* __restrict__ cell_inc, int C, int nz) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   unsigned int bits = 0;
   uint32_t key = 0xffffffffu;
@@ -120,10 +120,20 @@ __global__ void __launch_bounds__(256) k_apply(int n, float4* __restrict__ xs, f
   if (cell_inc) {
     // per-cell bound read by the next listed sweep (non-negative float bits
     // order like the values; NaN bits are above every finite value); the
-    // lanes of one cell combine first, since sorted neighbours share cells
+    // lanes of one cell combine first, since sorted neighbours share cells.
+    // Each cell's value also goes to its two z neighbours (the adjacent keys
+    // of its column), so an entry holds the largest increment over three
+    // cells of a column and a stencil needs nine entries, not 27.
     const unsigned peers = __match_any_sync(0xffffffffu, key);
     const unsigned m = __reduce_max_sync(peers, bits);
-    if (key != 0xffffffffu && m && (threadIdx.x & 31) == __ffs(peers) - 1) atomicMax(&cell_inc[key], m);
+    if (key != 0xffffffffu && m && (threadIdx.x & 31) == __ffs(peers) - 1) {
+      atomicMax(&cell_inc[key], m);
+      if ((int)key < C) {
+        const int z = (int)(key % (uint32_t)nz);
+        if (z > 0) atomicMax(&cell_inc[key - 1], m);
+        if (z < nz - 1) atomicMax(&cell_inc[key + 1], m);
+      }
+    }
   }
   block_max_bits_any(inc_bits, bits);
 }
@@ -137,7 +147,8 @@ gg_status apply(gg_system* S, int it, bool stab, bool last, cudaStream_t st) {
   const int ta = S->tune.apply_threads;
   k_apply<<<blocks_for(S->n, ta), ta, 0, st>>>((int)S->n, S->g.xs, S->g.pos[S->g.cur], S->g.delta,
                                                  S->g.s_extra, S->g.ncon, S->g.contacts, stab ? 1 : 0,
-                                                 last ? 1 : 0, &S->scal->inc_bits[it], S->g.keys, cell_inc);
+                                                 last ? 1 : 0, &S->scal->inc_bits[it], S->g.keys, cell_inc,
+                                                 S->grid.C, S->grid.nz);
   count_launches(S, 1);
   prof_end(S, PC_APPLY, S->n, st);
   GG_CUDA(cudaGetLastError());

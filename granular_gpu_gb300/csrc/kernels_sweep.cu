@@ -792,10 +792,29 @@ __device__ __forceinline__ bool nlist_bound_ok(const SweepArgs& a, float A) {
 }
 
 // Largest per-cell increment of the last sweep over the stencil of q and the
-// particle's own binning cell.
+// particle's own binning cell.  Every cell_inc entry holds the largest
+// increment over its cell and the cell's two z neighbours (k_apply), so the
+// stencil's 27 cells are covered by the nine entries of its columns at q.z;
+// the own cell adds its entry when it is not one of the 27 (the entry bounds
+// its increment from above).  A query cell outside the grid in z reads the
+// stencil's cells one by one (entries that may bound from above as well).
 __device__ __forceinline__ float nlist_cell_bound(const SweepArgs& a, int3 q, uint32_t own_key) {
   const Grid& g = a.g;
-  uint32_t m = a.cell_inc[own_key];
+  uint32_t m = 0u;
+  if (q.z >= 0 && q.z < g.nz) {
+    bool own_in = false;
+    for (int ox = -1; ox <= 1; ++ox)
+      for (int oy = -1; oy <= 1; ++oy) {
+        const int c = cell_key(g, q.x + ox, q.y + oy, q.z);
+        if (c == g.C) continue;
+        m = max(m, a.cell_inc[c]);
+        own_in |= own_key == (uint32_t)c || (own_key == (uint32_t)(c - 1) && q.z > 0) ||
+                  (own_key == (uint32_t)(c + 1) && q.z < g.nz - 1);
+      }
+    if (!own_in) m = max(m, a.cell_inc[own_key]);
+    return __uint_as_float(m);
+  }
+  m = a.cell_inc[own_key];
   for (int ox = -1; ox <= 1; ++ox)
     for (int oy = -1; oy <= 1; ++oy) {
       const int c0 = cell_key(g, q.x + ox, q.y + oy, q.z - 1);
@@ -810,9 +829,9 @@ __device__ __forceinline__ float nlist_cell_bound(const SweepArgs& a, int3 q, ui
 
 // Sweeps after the first: particles whose list is still exact run it; the
 // others are queued for k_sweep_nlist_build.
-template <int MM>
 // 5 resident blocks of 256 (48 registers; the per-target state carries no
 // double, and a few bytes spill): about 2 % faster than 4 blocks at 64.
+template <int MM>
 __global__ void __launch_bounds__(256, 5) k_sweep_nlist_keep(SweepArgs a) {
   const Grid& g = a.g;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -859,10 +878,10 @@ __global__ void __launch_bounds__(256, 5) k_sweep_nlist_keep(SweepArgs a) {
 // the queued ones later.
 constexpr int kBuildThreads = 128;
 
-template <int MM>
 // 8 resident blocks of 128 (64 registers, a few bytes spilled): the queued
 // rebuilds are latency-bound, and the extra warps hide more than the spills
 // cost (72 registers and 7 blocks measured 3 % slower over the sweeps).
+template <int MM>
 __global__ void __launch_bounds__(kBuildThreads, 8) k_sweep_nlist_build(SweepArgs a, int queued) {
   __shared__ int s_list[kBuildThreads / 32][kNlistMax][32];
   const Grid& g = a.g;
