@@ -73,6 +73,13 @@ __device__ __forceinline__ void for_each_stencil_column_until(const Grid& g, int
   }
 }
 
+// n / d with the constants of make_udiv (d >= 1).
+__device__ __forceinline__ uint32_t udiv(uint32_t n, const UDiv& u) {
+  if (u.d <= 1) return n;
+  const uint32_t t = __umulhi(u.m, n);
+  return (t + ((n - t) >> 1)) >> u.s;
+}
+
 // sqrtf(dd) > X, with the clear cases decided from dd against X*X: beyond
 // a relative margin of 2e-6 on the square the rounded root lies several
 // ulps from X.  Near-ties, and X*X outside the normal range, take the root.

@@ -19,6 +19,26 @@ struct Grid {
   int C;  // nx*ny*nz; the out-of-grid key
 };
 
+// Unsigned 32-bit division by an invariant d with a multiply-high
+// (Granlund and Montgomery, "Division by invariant integers using
+// multiplication", 1994; the round-up variant with a 33-bit multiplier):
+// n / d = (hi(m n) + ((n - hi(m n)) >> 1)) >> s for every 32-bit n, d >= 2.
+struct UDiv {
+  uint32_t m = 0;
+  int s = 0;
+  uint32_t d = 1;
+};
+inline UDiv make_udiv(uint32_t d) {
+  UDiv u;
+  u.d = d;
+  if (d <= 1) return u;
+  int l = 0;
+  while (((uint64_t)1 << l) < d) ++l;  // ceil(log2 d)
+  u.m = (uint32_t)((((uint64_t)1 << 32) * (((uint64_t)1 << l) - d)) / d + 1);
+  u.s = l - 1;
+  return u;
+}
+
 // Scalars that live on the device so a substep needs no host round trip.
 struct DevScalars {
   unsigned int rmax_bits;      // max contact radius (float bits), this step

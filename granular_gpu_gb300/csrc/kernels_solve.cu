@@ -83,7 +83,7 @@ __global__ void __launch_bounds__(256) k_apply(int n, float4* __restrict__ xs, f
                         const float4* __restrict__ delta, int32_t* __restrict__ s_extra,
                         int32_t* __restrict__ ncon, int32_t* __restrict__ contacts, int stab, int last,
                         unsigned int* __restrict__ inc_bits, const uint32_t* __restrict__ keys,
-                        uint32_t* __restrict__ cell_inc, int C, int nz) {
+                        uint32_t* __restrict__ cell_inc, int C, int nz, UDiv div_z) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   unsigned int bits = 0;
   uint32_t key = 0xffffffffu;
@@ -129,7 +129,7 @@ __global__ void __launch_bounds__(256) k_apply(int n, float4* __restrict__ xs, f
     if (key != 0xffffffffu && m && (threadIdx.x & 31) == __ffs(peers) - 1) {
       atomicMax(&cell_inc[key], m);
       if ((int)key < C) {
-        const int z = (int)(key % (uint32_t)nz);
+        const int z = (int)(key - udiv(key, div_z) * (uint32_t)nz);
         if (z > 0) atomicMax(&cell_inc[key - 1], m);
         if (z < nz - 1) atomicMax(&cell_inc[key + 1], m);
       }
@@ -148,7 +148,7 @@ gg_status apply(gg_system* S, int it, bool stab, bool last, cudaStream_t st) {
   k_apply<<<blocks_for(S->n, ta), ta, 0, st>>>((int)S->n, S->g.xs, S->g.pos[S->g.cur], S->g.delta,
                                                  S->g.s_extra, S->g.ncon, S->g.contacts, stab ? 1 : 0,
                                                  last ? 1 : 0, &S->scal->inc_bits[it], S->g.keys, cell_inc,
-                                                 S->grid.C, S->grid.nz);
+                                                 S->grid.C, S->grid.nz, make_udiv((uint32_t)S->grid.nz));
   count_launches(S, 1);
   prof_end(S, PC_APPLY, S->n, st);
   GG_CUDA(cudaGetLastError());

@@ -57,6 +57,7 @@ struct SweepArgs {
   int cap;
   float skin;
   float eabs;    // bound on the rounding of one position update
+  UDiv div_yz, div_z;  // division by ny * nz and by nz (binning cell of a key)
   // batched scenes: scene of a particle = its x* slab, floor(x / width);
   // each scene has its own friction cap (null: a.fcap for every particle)
   const float* __restrict__ scene_fcap;
@@ -124,10 +125,9 @@ __device__ __forceinline__ void make_target_lite(const SweepArgs& a, int i, floa
   t.binned = (int)key < g.C;
   t.cx = t.cy = t.cz = 0;
   if (t.binned) {
-    const int nyz = g.ny * g.nz;
-    t.cx = (int)key / nyz;
-    const int r = (int)key - t.cx * nyz;
-    t.cy = r / g.nz;
+    t.cx = (int)udiv(key, a.div_yz);
+    const int r = (int)key - t.cx * g.ny * g.nz;
+    t.cy = (int)udiv((uint32_t)r, a.div_z);
     t.cz = r - t.cy * g.nz;
   }
 }
@@ -997,6 +997,8 @@ gg_status sweep(gg_system* S, int it, cudaStream_t st) {
   a.cell_inc = S->g.cell_inc;
   a.cap = (int)S->cap;
   a.skin = S->nl_skin;
+  a.div_yz = make_udiv((uint32_t)(S->grid.ny * S->grid.nz));
+  a.div_z = make_udiv((uint32_t)S->grid.nz);
   {
     // half an ulp of the largest in-grid coordinate, with a margin
     const float ext = S->grid.L * (float)std::max(S->grid.nx, std::max(S->grid.ny, S->grid.nz));
