@@ -152,6 +152,31 @@ def cpu_sample(steps: int, warmup: int, fp64: bool = True):
     return units / dt, threads, dt
 
 
+def fp64_error(device: int) -> dict:
+    """The library (FP32, CUDA's own math functions) against the serial FP64
+    restatement after one substep (the constructor's) from the same state of
+    the bounded sample: max |x - x_fp64| in units of r and max |v - v_fp64|.
+    (After a second grid build the two sort particles near cell faces
+    differently, so particles compare index by index after one substep.)"""
+    import granular_gpu_gb300 as gg
+    from granular_gpu_gb300 import abi, workloads
+    from oracle import oracle as orc
+    desc = workloads.column_collapse(counts=SAMPLE_COUNTS)
+    s = gg.GranularSystem(**workloads.system_kwargs(desc), device=device)
+    o = orc.OracleSystem(desc, fp64=True)
+    if s.size() != o.size():
+        out = {"unavailable": f"particle counts differ ({s.size()} vs {o.size()})"}
+    else:
+        r = 0.002
+        dx = np.abs(s.read(gg.FIELD_POS).astype(np.float64) - o.read(abi.FIELD_POS).astype(np.float64)).max()
+        dv = np.abs(s.read(gg.FIELD_VEL).astype(np.float64) - o.read(abi.FIELD_VEL).astype(np.float64)).max()
+        out = {"pos_max_abs_r": float(dx / r), "vel_max_abs": float(dv), "substeps": 1,
+               "sample": "64x64x64 sub-lattice of the column scene, FP32 CUDA math against the FP64 build"}
+    s.close()
+    o.close()
+    return out
+
+
 def run_reference(args):
     rank, world, _ = _dist()
     if rank != 0:
@@ -376,6 +401,7 @@ def run_mine(args):
         cv, threads, _ = cpu_sample(steps=args.cpu_steps, warmup=1)
         line["cpu_baseline"] = {"value": cv, "unit": METRIC, "cores": threads, "kind": "port",
                                 "sample": SAMPLE_NOTE + f", {args.cpu_steps} timed substeps, FP64 build"}
+        line["fp64_error"] = fp64_error(local)
     sysg.close()
     if rank == 0:
         print(json.dumps(line), flush=True)
