@@ -104,6 +104,48 @@ def test_box_drop_substeps_match_oracle():
     assert s.read(gg.FIELD_CONTACTS).sum() > 0, "the test scene must produce contacts"
 
 
+def _edge_scene(name):
+    d = workloads.box_drop(n_side=6, substeps=4, iters=3, adaptive=1, upsample_per=4)
+    if name == "no_particles":
+        d.update(particles=np.zeros((0, 3), np.float32), n_particles=0, upsampled=None, n_upsampled=0)
+    elif name == "one_particle":
+        p = np.array([[0.5, 0.3, 0.5]], np.float32)
+        d.update(particles=p, n_particles=1, upsampled=np.repeat(p, 4, 0) + np.float32(0.001), n_upsampled=4)
+    elif name == "all_out_of_grid":
+        # the block starts below the grid (y < 0): every key is the
+        # out-of-grid sentinel, nothing meets a wall or a partner
+        p = d["particles"].copy()
+        p[:, 1] -= 1.0
+        d.update(particles=p, upsampled=None, n_upsampled=0)
+    elif name == "no_walls":
+        d.update(boundary=np.zeros((0, 3), np.float32), n_boundary=0)
+    elif name == "ragged_cells":
+        # a few particles far apart, one dense clump and one on the grid's
+        # upper corner: cells of 0, 1 and many particles side by side
+        rng = np.random.default_rng(5)
+        clump = (np.float32(0.5) + rng.uniform(-0.012, 0.012, (40, 3))).astype(np.float32)
+        lone = np.array([[0.1, 0.9, 0.1], [0.9, 0.5, 0.9], [0.999, 0.999, 0.999]], np.float32)
+        p = np.concatenate([clump, lone])
+        d.update(particles=p, n_particles=p.shape[0],
+                 upsampled=np.repeat(p, 4, 0) + np.float32(0.002), n_upsampled=4 * p.shape[0])
+    return d
+
+
+@pytest.mark.parametrize("name", ["no_particles", "one_particle", "all_out_of_grid", "no_walls", "ragged_cells"])
+def test_edge_scenes_match_oracle(name):
+    # empty and ragged inputs through the whole substep (grid, sweeps,
+    # upsampling, merge/split), bit-exact against the oracle
+    s, o = _pair(_edge_scene(name))
+    _compare(s, o, 0)
+    for k in range(1, 7):
+        s.step(1)
+        o.step(1)
+        _compare(s, o, k)
+        assert s.upsampled_size() == o.size(abi.SET_UPSAMPLED)
+        if s.upsampled_size():
+            assert np.array_equal(s.read(gg.FIELD_POS, gg.SET_UPSAMPLED), o.read(abi.FIELD_POS, abi.SET_UPSAMPLED))
+
+
 @pytest.mark.parametrize("variant,other", [(0, 0), (1, 1), (2, 0), (3, 0), (4, 1), (6, 0)])
 def test_sweep_variants_bit_exact(variant, other):
     # sweep variants 0-6 (see kernels_sweep.cu); surface/distance/merge/
