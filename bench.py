@@ -108,6 +108,32 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
+def stream_kernels(prof: dict, desc: dict, peak: float) -> dict:
+    """The HBM-bound grid classes, timed live like the dominant kernel:
+    algorithmic bytes per unit (P radix passes of 8 bits over keys up to C:
+    16 B per scatter pass, 4 B per histogram pass after the first, whose
+    digits the hash kernel counts), achieved GB/s and the fraction of the
+    measured copy bandwidth."""
+    passes = max(1, -(-int(np.prod(desc["cell_size"])).bit_length() // 8))
+    sort_b = 16 * passes + 4 * (passes - 1)
+    basis = {
+        "hash": (24, "particle", "read position 16 B, write key and index 8 B"),
+        "sort": (sort_b, "particle", f"{passes} scatter passes of key and index, {passes - 1} histogram passes"),
+        "reorder": (124, "particle", "gather 9 per-particle fields by the permutation (read and write)"),
+        "up_grid": (24 + sort_b + 68, "render point",
+                    "hash 24 B, sort, then gather index 4 B and position and velocity 32 B in, 32 B out"),
+    }
+    out = {}
+    for k, (b, unit, note) in basis.items():
+        v = prof.get(k)
+        if not v or not v["launches"] or v["ms"] <= 0:
+            continue
+        gbs = b * v["units"] / (v["ms"] / 1e3) / 1e9
+        out[k] = {"bytes_per_unit": b, "unit_of_work": unit, "bytes_basis": note,
+                  "achieved_gbs": round(gbs, 1), "frac": round(gbs / peak, 3)}
+    return out
+
+
 def ncu_traffic(cls: str):
     """DRAM bytes per launch of a kernel class from one ncu capture
     (dram__bytes_read.sum + dram__bytes_write.sum) and the units that launch
@@ -360,7 +386,8 @@ def run_mine(args):
                      # bound by instruction issue, not by HBM
                      "issue_active_pct": (tr or {}).get("issue_active_pct"),
                      "sm_throughput_pct": (tr or {}).get("sm_throughput_pct"),
-                     "list_builds_per_particle_sweep": list_builds / max(prof["sweep"]["units"], 1)},
+                     "list_builds_per_particle_sweep": list_builds / max(prof["sweep"]["units"], 1),
+                     "stream_kernels": stream_kernels(prof, desc, peak)},
         "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d // max(args.steps, 1),
                 "d2h_bytes_per_step": d2h // max(args.steps, 1)},
         "gpu_launches": int(launches),
