@@ -166,7 +166,7 @@ struct Tuning {
   int predict_threads = 256;
   int apply_threads = 256;
   int finalize_threads = 256;
-  int keep_threads = 256;
+  int keep_threads = 128;  // gg_autotune chose 128 on the column, the pile and the batched scenes
   int build_blocks_per_sm = 16;
   int sweep_variant = 0;  // variant of the default sweep: 0 contact lists, 1 pruned stencil sweep
 };
