@@ -713,7 +713,7 @@ gg_status gg_grid_create(int32_t device, int64_t capacity, const int32_t cell_si
   REQUIRE(out && cell_size && capacity > 0 && cell_length > 0, "gg_grid_create: invalid argument");
   REQUIRE(cell_size[0] > 0 && cell_size[1] > 0 && cell_size[2] > 0, "gg_grid_create: cell_size must be positive");
   const int64_t C64 = (int64_t)cell_size[0] * cell_size[1] * cell_size[2];
-  REQUIRE(C64 < ((int64_t)1 << 30) && capacity < ((int64_t)1 << 31) - 1, "gg_grid_create: grid or capacity too large");
+  REQUIRE(C64 < ((int64_t)1 << 30) && capacity <= kMaxCount, "gg_grid_create: grid or capacity too large");
   GG_CUDA(cudaSetDevice(device));
   gg_grid* g = new gg_grid();
   g->device = device;

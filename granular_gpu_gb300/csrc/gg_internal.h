@@ -62,6 +62,9 @@ constexpr int kMaxSweeps = 256;  // sweeps per substep (stabilisation + Jacobi)
 
 enum ErrorBits { ERR_CAPACITY = 1, ERR_NUMERIC = 2, ERR_TIMEOUT = 4 };
 
+// Largest element count of a set: launches round counts up to whole tiles
+// of at most 4,096 items and index them with signed 32-bit integers.
+constexpr int64_t kMaxCount = ((int64_t)1 << 31) - ((int64_t)1 << 16);
 constexpr int kNlistMax = 32;  // contact candidates kept per particle
 
 // Kernel classes timed by gg_profile_*.

@@ -259,9 +259,10 @@ gg_status system_create(const gg_desc* d, gg_system** out) {
   }
   int64_t cap = d->max_particles > 0 ? d->max_particles : 2 * d->n_particles;
   cap = std::max<int64_t>(cap, std::max<int64_t>(d->n_particles, 1));
-  if (cap >= ((int64_t)1 << 31) - 1 || d->n_upsampled >= ((int64_t)1 << 31) - 1 ||
-      d->n_boundary >= ((int64_t)1 << 31) - 1) {
-    set_error("gg_create: particle counts must stay below 2^31");
+  // a launch rounds its count up to whole tiles (at most 4,096 items), and
+  // thread and tile indices are signed 32-bit: counts stay 2^16 below 2^31
+  if (cap > kMaxCount || d->n_upsampled > kMaxCount || d->n_boundary > kMaxCount) {
+    set_error("gg_create: particle counts must not exceed 2^31 - 2^16");
     return GG_ERR_INVALID_ARGUMENT;
   }
   GG_CUDA(cudaSetDevice(d->device));

@@ -166,7 +166,8 @@ typedef struct gg_desc {
   int32_t is_adaptive;
   int32_t skip_initial_step;   /* 0 = the constructor runs one step (GranularSystem.cu:62) */
   int32_t device;              /* CUDA device ordinal */
-  int64_t max_particles;       /* granular capacity; 0 = 2 x n_particles */
+  int64_t max_particles;       /* granular capacity; 0 = 2 x n_particles.  Capacity, n_upsampled
+                                  and n_boundary are each at most 2^31 - 2^16 */
   void* stream;                /* optional cudaStream_t to run on; NULL = own stream */
   gg_params params;
 } gg_desc;

@@ -75,6 +75,17 @@ def test_invalid_arguments_are_reported_without_a_gpu():
     d.params = abi.default_params()
     d.params.iters = 100
     assert lib.gg_create(C.byref(d), C.byref(h)) == abi.GG_ERR_INVALID_ARGUMENT
+    d.params = abi.default_params()
+    # counts past 2^31 - 2^16 (launch grids round up to whole tiles of
+    # signed 32-bit indices) are refused before any device work
+    limit = (1 << 31) - (1 << 16)
+    d.upsampled = d.particles
+    d.n_upsampled = limit + 1
+    assert lib.gg_create(C.byref(d), C.byref(h)) == abi.GG_ERR_INVALID_ARGUMENT
+    assert b"2^31" in lib.gg_last_error()
+    d.n_upsampled = 0
+    d.max_particles = limit + 1
+    assert lib.gg_create(C.byref(d), C.byref(h)) == abi.GG_ERR_INVALID_ARGUMENT
     assert lib.gg_step(None, 1) == abi.GG_ERR_INVALID_ARGUMENT
 
 
