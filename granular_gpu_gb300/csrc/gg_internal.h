@@ -104,6 +104,8 @@ struct Granular {
   float* nl_acc = nullptr;    // displacement bound summed since the particle's list build
   int32_t* nl_queue = nullptr; // particles whose list is rebuilt in this sweep
   uint32_t* cell_inc = nullptr; // per cell (C+1): max |x* increment| of its particles in the last sweep (float bits)
+  float* ld_sum = nullptr;       // surface pass: mass within the merge radius, in candidate order
+  int32_t* ld_cnt = nullptr;     // and the count (-1: not computed there)
   // grid
   uint32_t* keys = nullptr;   // sorted keys of the last build
   uint32_t* perm = nullptr;   // sort permutation of the last build

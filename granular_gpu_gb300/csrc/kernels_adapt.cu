@@ -41,10 +41,12 @@ __device__ __forceinline__ unsigned surface_chunk_mask(const float4* __restrict_
 __constant__ int kTowards[9][2] = {{1, 1}, {1, 0}, {0, 1}, {0, 0}, {1, -1}, {-1, 1}, {0, -1}, {-1, 0}, {-1, -1}};
 
 template <int MM>
-__global__ void __launch_bounds__(256) k_surface(Grid g, int n, const float4* __restrict__ pos,
+__global__ void __launch_bounds__(256, 6) k_surface(Grid g, int n, const float4* __restrict__ pos,
                                                  const float* __restrict__ rs, const int32_t* __restrict__ cs,
                                                  int32_t* __restrict__ surface, float cone, float cos_cone,
-                                                 int min_nb, const unsigned int* __restrict__ rmax_bits) {
+                                                 int min_nb, const unsigned int* __restrict__ rmax_bits,
+                                                 const float* __restrict__ mass, float merge_cut,
+                                                 float* __restrict__ ld_sum, int32_t* __restrict__ ld_cnt) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const float3 xi = f3(pos[i]);
@@ -54,6 +56,14 @@ __global__ void __launch_bounds__(256) k_surface(Grid g, int n, const float4* __
   const float R2 = Rw * Rw;
   float3 cv = make_float3(0.f, 0.f, 0.f);
   unsigned nn = 0;
+  // The merge scan's local density (merge_mark_gpu, Solver.cu:526-653): the
+  // mass within the merge radius, the particle itself included, summed in
+  // candidate order.  Taken here when the prefilter reaches the merge
+  // radius (its cut with the merge scan's own margin), so that the merge
+  // scan only looks at candidates after i.
+  const bool ldc = ld_cnt && merge_cut * 1.0001f <= R2;
+  float ld = 0.0f;
+  int lc = 0;
   // Each stencil column is scanned in chunks of 32: the prefilter marks
   // the candidates that may lie within 2 (r_i + r_j) in a mask, and the
   // exact test and the sums run over the marked ones in candidate order.
@@ -61,16 +71,27 @@ __global__ void __launch_bounds__(256) k_surface(Grid g, int n, const float4* __
     const int j1 = cs[k0 + nc];
     for (int c0 = cs[k0]; c0 < j1; c0 += 32) {
       unsigned mask = surface_chunk_mask(pos, c0, min(32, j1 - c0), i, xi, R2);
+      const unsigned self = (unsigned)(i - c0);
+      if (ldc && self < 32u) mask |= 1u << self;
       while (mask) {
         const int j = c0 + __ffs(mask) - 1;
         mask &= mask - 1u;
         const float3 d = sub3(xi, f3(pos[j]));
-        if (sqrt_gt(dot3(d, d), 2.0f * (ri + rs[j]))) continue;
+        const float dd = dot3(d, d);
+        if (ldc && dd < merge_cut) {
+          ld += mass[j];
+          ++lc;
+        }
+        if (j == i || sqrt_gt(dd, 2.0f * (ri + rs[j]))) continue;
         cv = add3(cv, m_normalize3<MM>(d));
         ++nn;
       }
     }
   });
+  if (ld_cnt) {
+    ld_sum[i] = ld;
+    ld_cnt[i] = ldc ? lc : -1;
+  }
   if (nn <= (unsigned)min_nb) {
     surface[i] = 1;
     return;
@@ -170,15 +191,20 @@ __global__ void __launch_bounds__(256) k_surface_warp(Grid g, int n, const float
   if (valid) surface[i] = (nn <= (unsigned)min_nb || !vote) ? 1 : 0;
 }
 
+void merge_cuts(const gg_system* S, float& f_out, float& T_out);
+
 gg_status surface(gg_system* S, cudaStream_t st) {
   if (S->n <= 0) return GG_OK;
   const int c = S->g.cur;
   prof_begin(S, PC_SURFACE, st);
   if (S->P.reserved[1] != 1) {
     auto kern = S->P.math_mode ? k_surface<1> : k_surface<0>;
+    float merge_f = 0.0f, merge_cut = 0.0f;
+    merge_cuts(S, merge_f, merge_cut);
     kern<<<blocks_for(S->n, 256), 256, 0, st>>>(S->grid, (int)S->n, S->g.pos[c], S->g.rs[c], S->g.cell_start,
                                                  S->g.surface, S->P.surface_cone, std::cos(S->P.surface_cone),
-                                                 S->P.surface_min_neighbors, &S->scal->rmax_bits);
+                                                 S->P.surface_min_neighbors, &S->scal->rmax_bits, S->g.mass[c],
+                                                 merge_cut, S->g.ld_sum, S->g.ld_cnt);
   } else {
     auto kern = S->P.math_mode ? k_surface_warp<1> : k_surface_warp<0>;
     kern<<<blocks_for(S->n, 256), 256, 0, st>>>(S->grid, (int)S->n, S->g.pos[c], S->g.rs[c], S->g.cell_start,
@@ -309,6 +335,8 @@ struct MergeArgs {
   double merge_radius;
   float merge_radius_f;  // smallest float above merge_radius: dis < r (double) <=> dis < this
   float merge_r2_cut;    // smallest float whose sqrtf reaches merge_radius_f: dis < it <=> dd < this
+  const float* __restrict__ ld_sum;    // density sums of the surface pass, or null
+  const int32_t* __restrict__ ld_cnt;
 };
 
 // merge_mark_gpu (Solver.cu:526-653), scan phase: every thread's neighbour
@@ -328,9 +356,18 @@ __global__ void __launch_bounds__(256) k_merge_scan(MergeArgs a) {
   int lc = 0;
   const bool sd_bug = a.sdist[i] < a.sdt;  // Solver.cu:578 tests [i]: always false here
   const float pre_cut = a.merge_r2_cut * 1.0001f;
+  // With the density taken by the surface pass, only the partners j > i
+  // are looked at: the particles are sorted by cell, so they are the
+  // candidates from index i + 1 on, visited in the same order.
+  const int pre_lc = a.ld_cnt ? a.ld_cnt[i] : -1;
+  const bool dens_done = pre_lc >= 0;
+  if (dens_done) {
+    ld = a.ld_sum[i];
+    lc = pre_lc;
+  }
   for_each_stencil_column(a.g, q, [&](int k0, int nc) {
     const int j1 = min(a.cs[k0 + nc], a.n);
-    for (int c0 = a.cs[k0]; c0 < j1; c0 += 32) {
+    for (int c0 = dens_done ? max(a.cs[k0], i + 1) : a.cs[k0]; c0 < j1; c0 += 32) {
       // candidates clearly beyond the merge radius (a fused dot product
       // against the cut with a margin far above its rounding) add nothing:
       // the chunk's mask marks the others, visited in candidate order
@@ -349,7 +386,7 @@ __global__ void __launch_bounds__(256) k_merge_scan(MergeArgs a) {
         // dis < merge radius (as a float) <=> dd below the smallest square
         // whose rounded root reaches it
         const bool inr = dd < a.merge_r2_cut;
-        if (inr) {
+        if (inr && !dens_done) {
           ld += a.mass[j];
           ++lc;
         }
@@ -471,6 +508,27 @@ __global__ void k_merge_apply(MergeArgs a) {
   a.merge_vel[t] = make_float4(mv.x, mv.y, mv.z, 0.f);
 }
 
+// The merge radius as float thresholds: f, the smallest float at or above
+// merge_radius (dis < r in double <=> dis < f), and T, the smallest float
+// whose rounded root reaches f (sqrtf(dd) < f <=> dd < T).
+void merge_cuts(const gg_system* S, float& f_out, float& T_out) {
+  float f = (float)S->P.merge_radius;
+  if ((double)f < S->P.merge_radius) f = nextafterf(f, INFINITY);
+  // dis < r_d  <=>  dis < f when f is the smallest float >= r_d and f != r_d;
+  // when f == r_d exactly the comparison is already exact.
+  // sqrtf is correctly rounded and monotone here and on the device, so
+  // sqrtf(dd) < f  <=>  dd < T for the smallest float T with sqrtf(T) >= f.
+  float T = (float)((double)f * (double)f);
+  if (!(f > 0.0f)) T = 0.0f;  // no distance is below it (NaN included)
+  else if (!std::isfinite(T)) T = INFINITY;
+  else {
+    while (T > 0.0f && std::sqrt(nextafterf(T, 0.0f)) >= f) T = nextafterf(T, 0.0f);
+    while (std::sqrt(T) < f) T = nextafterf(T, INFINITY);
+  }
+  f_out = f;
+  T_out = T;
+}
+
 gg_status merge_mark(gg_system* S, cudaStream_t st) {
   if (S->n <= 0) return GG_OK;
   const int c = S->g.cur;
@@ -496,24 +554,11 @@ gg_status merge_mark(gg_system* S, cudaStream_t st) {
   a.sdt = S->P.surface_dist_threshold;
   a.target_density = S->P.target_density;
   a.merge_radius = S->P.merge_radius;
-  {
-    // float threshold equivalent to the double comparison dis < merge_radius
-    float f = (float)S->P.merge_radius;
-    if ((double)f < S->P.merge_radius) f = nextafterf(f, INFINITY);
-    a.merge_radius_f = f;
-    // dis < r_d  <=>  dis < f when f is the smallest float >= r_d and f != r_d;
-    // when f == r_d exactly the comparison is already exact.
-    // sqrtf is correctly rounded and monotone here and on the device, so
-    // sqrtf(dd) < f  <=>  dd < T for the smallest float T with sqrtf(T) >= f.
-    float T = (float)((double)f * (double)f);
-    if (!(f > 0.0f)) T = 0.0f;  // no distance is below it (NaN included)
-    else if (!std::isfinite(T)) T = INFINITY;
-    else {
-      while (T > 0.0f && std::sqrt(nextafterf(T, 0.0f)) >= f) T = nextafterf(T, 0.0f);
-      while (std::sqrt(T) < f) T = nextafterf(T, INFINITY);
-    }
-    a.merge_r2_cut = T;
-  }
+  merge_cuts(S, a.merge_radius_f, a.merge_r2_cut);
+  // the one-thread scan takes the density sums of the surface pass, which
+  // runs the same variant switch
+  a.ld_sum = S->P.reserved[1] != 1 ? S->g.ld_sum : nullptr;
+  a.ld_cnt = S->P.reserved[1] != 1 ? S->g.ld_cnt : nullptr;
   const int nb = blocks_for(S->n, 256);
   prof_begin(S, PC_MERGE, st);
   if (S->P.reserved[1] != 1) k_merge_scan<<<nb, 256, 0, st>>>(a);

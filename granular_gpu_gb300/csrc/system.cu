@@ -209,7 +209,7 @@ static void free_all(gg_system* S) {
   }
   void* ptrs[] = {G.merge_vel, G.surface, G.sdist, G.cover, G.xs, G.inv_m, G.delta, G.s_extra, G.contacts,
                   G.ncon, G.keys, G.perm, G.cell_start, G.cell_surf, G.prop, G.ldens, G.winner, G.split_flag, G.keep_flag,
-                  G.split_slot, G.keep_slot, G.child_pos, G.nl_idx, G.nl_meta, G.nl_acc, G.nl_queue, G.cell_inc, S->b.pos, S->b.animated, S->b.pos_alt,
+                  G.split_slot, G.keep_slot, G.child_pos, G.nl_idx, G.nl_meta, G.nl_acc, G.nl_queue, G.cell_inc, G.ld_sum, G.ld_cnt, S->b.pos, S->b.animated, S->b.pos_alt,
                   S->b.animated_alt, S->b.keys, S->b.perm, S->b.cell_start, S->u.keys, S->u.perm, S->scal,
                   S->stats_partial, S->stage, S->feat, S->xs0, S->warm_target, S->scene_fcap,
                   S->scene_acc};
@@ -312,7 +312,7 @@ gg_status system_create(const gg_desc* d, gg_system** out) {
   ALLOC(G.contacts, cap); ALLOC(G.ncon, cap); ALLOC(G.keys, cap); ALLOC(G.perm, cap);
   ALLOC(G.cell_start, C1); ALLOC(G.cell_surf, C1); ALLOC(G.prop, cap); ALLOC(G.ldens, cap); ALLOC(G.winner, cap);
   ALLOC(G.split_flag, cap); ALLOC(G.keep_flag, cap); ALLOC(G.split_slot, cap); ALLOC(G.keep_slot, cap);
-  ALLOC(G.child_pos, cap);
+  ALLOC(G.child_pos, cap); ALLOC(G.ld_sum, cap); ALLOC(G.ld_cnt, cap);
   // contact lists: a negative skin asks for the automatic one, a tenth of
   // the cell length; zero or NaN turns them off
   S->nl_skin = S->P.nlist_skin < 0.0f ? 0.1f * S->grid.L : S->P.nlist_skin;
