@@ -725,6 +725,10 @@ struct CompactArgs {
 // A split parent keeps half of its mass (Solver.cu:816-826).
 template <int MM>
 __global__ void k_compact(CompactArgs a) {
+  // nothing removed and nothing split: the compaction would copy every
+  // particle to its own slot, so the state stays where it is (the host
+  // keeps the current buffers, from the same two counts)
+  if (a.scal->n_kept == a.n && a.scal->n_split == 0) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
   if (a.remove[i] == 1) return;
@@ -829,7 +833,8 @@ gg_status split_and_compact(gg_system* S, cudaStream_t st) {
   k_adapt_counts<<<1, 1, 0, st>>>(S->scal, (int)S->n, (int)S->cap);
   count_launches(S, 2);
   prof_end(S, PC_COMPACT, S->n, st);
-  G.cur = o;
+  // the caller switches to the other buffers once it has read the counts
+  // (unless the compaction was the identity)
   GG_CUDA(cudaGetLastError());
   return GG_OK;
 }

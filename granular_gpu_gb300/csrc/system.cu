@@ -170,6 +170,8 @@ gg_status step_once(gg_system* S) {
     GG_CUDA(cudaMemcpyAsync(S->scal_host, S->scal, sizeof(DevScalars), cudaMemcpyDeviceToHost, st));
     GG_CUDA(cudaStreamSynchronize(st));
     const int64_t before = S->n;
+    // k_compact wrote the other buffers unless nothing was removed or split
+    if (!(S->scal_host->n_kept == before && S->scal_host->n_split == 0)) S->g.cur ^= 1;
     S->n = S->scal_host->n_after;
     S->merged_last = S->scal_host->n_removed;
     S->split_last = S->scal_host->n_split;
