@@ -270,8 +270,6 @@ def run_mine(args):
     desc = workloads.column_collapse(counts=counts, seed=42 + rank)
     if args.math_mode:
         desc["params"].math_mode = args.math_mode
-    desc["params"].reserved[0] = args.sweep_variant
-    desc["params"].reserved[1] = args.stencil_variant
     if args.nlist_skin is not None:
         desc["params"].nlist_skin = args.nlist_skin * 0.002
     n0 = desc["n_particles"]
@@ -455,15 +453,9 @@ def main():
     ap.add_argument("--counts", default="128,256,256",
                     help="column lattice x,y,z (the benchmark workload is 128,256,256)")
     ap.add_argument("--math-mode", type=int, default=0)
-    ap.add_argument("--sweep-variant", type=int, default=0,
-                    help="0 default (contact lists), 1 pruned per particle, 2 shared-memory tile, "
-                         "3 per particle with deferred contacts, 4 warp staged, 5 contact lists, "
-                         "6 warp-cooperative")
     ap.add_argument("--nlist-skin", type=float, default=None,
                     help="contact-list skin in radii of 0.002 (default: a tenth of the cell length; "
                          "0 turns the lists off)")
-    ap.add_argument("--stencil-variant", type=int, default=0,
-                    help="surface/distance/merge/upsampling: 0 one thread per particle, 1 warp-cooperative")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -271,6 +271,23 @@ class GranularSystem:
         _check(lib().gg_autotune(self._h, substeps, C.byref(t)))
         return {k: getattr(t, k) for k, _ in abi.gg_tuning._fields_ if k != "pad_"}
 
+    def tuning(self) -> dict:
+        """gg_get_tuning: the launch shapes and default-sweep variant in use."""
+        t = abi.gg_tuning()
+        _check(lib().gg_get_tuning(self._h, C.byref(t)))
+        return {k: getattr(t, k) for k, _ in abi.gg_tuning._fields_ if k != "pad_"}
+
+    def set_tuning(self, **changes):
+        """gg_set_tuning: change some launch shapes (for example the ones an
+        earlier autotune chose); results do not depend on them."""
+        t = abi.gg_tuning()
+        _check(lib().gg_get_tuning(self._h, C.byref(t)))
+        for k, v in changes.items():
+            if k not in dict(abi.gg_tuning._fields_):
+                raise KeyError(k)
+            setattr(t, k, v)
+        _check(lib().gg_set_tuning(self._h, C.byref(t)))
+
     def set_warm_start(self, mlp=None):
         """gg_set_warm_start: attach a network (gg_params.warm_start = 1) or,
         with None, only allocate the buffers of the recording mode (2)."""

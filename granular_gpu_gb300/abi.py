@@ -84,7 +84,7 @@ class gg_params(C.Structure):
         ("mass_ledger", C.c_int32), ("merge_enabled", C.c_int32),
         ("upsample_enabled", C.c_int32), ("math_mode", C.c_int32), ("nlist_skin", C.c_float),
         ("target_residual", C.c_float), ("max_sweeps", C.c_int32), ("warm_start", C.c_int32),
-        ("warm_start_scale", C.c_float), ("reserved", C.c_int32 * 2),
+        ("warm_start_scale", C.c_float),
     ]
 
 
@@ -233,6 +233,8 @@ SIGNATURES = {
     "gg_graph_capture": (C.c_int, [P_, C.c_int32]),
     "gg_graph_launch": (C.c_int, [P_]),
     "gg_autotune": (C.c_int, [P_, C.c_int32, C.POINTER(gg_tuning)]),
+    "gg_get_tuning": (C.c_int, [P_, C.POINTER(gg_tuning)]),
+    "gg_set_tuning": (C.c_int, [P_, C.POINTER(gg_tuning)]),
     "gg_set_params": (C.c_int, [P_, C.POINTER(gg_params)]),
 }
 

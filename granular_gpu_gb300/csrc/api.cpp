@@ -911,3 +911,40 @@ gg_status gg_autotune(gg_system* S, int32_t substeps, gg_tuning* out) {
   return GG_OK;
   GG_GUARD_END
 }
+
+gg_status gg_get_tuning(gg_system* S, gg_tuning* out) {
+  GG_GUARD_BEGIN
+  REQUIRE(S && out, "gg_get_tuning: null argument");
+  const Tuning& T = S->tune;
+  std::memset(out, 0, sizeof(*out));
+  out->predict_threads = T.predict_threads;
+  out->apply_threads = T.apply_threads;
+  out->finalize_threads = T.finalize_threads;
+  out->keep_threads = T.keep_threads;
+  out->build_blocks_per_sm = T.build_blocks_per_sm;
+  out->sweep_variant = T.sweep_variant;
+  return GG_OK;
+  GG_GUARD_END
+}
+
+gg_status gg_set_tuning(gg_system* S, const gg_tuning* t) {
+  GG_GUARD_BEGIN
+  REQUIRE(S && t, "gg_set_tuning: null argument");
+  REQUIRE(!S->graph_exec, "gg_set_tuning: set launch shapes before capturing a graph");
+  auto threads_ok = [](int v) { return v >= 32 && v <= 1024 && v % 32 == 0; };
+  REQUIRE(threads_ok(t->predict_threads) && threads_ok(t->apply_threads) && threads_ok(t->finalize_threads) &&
+              threads_ok(t->keep_threads),
+          "gg_set_tuning: threads per block must be a multiple of 32 in 32..1024");
+  REQUIRE(t->build_blocks_per_sm >= 1 && t->build_blocks_per_sm <= 32,
+          "gg_set_tuning: build_blocks_per_sm must be in 1..32");
+  REQUIRE(t->sweep_variant == 0 || t->sweep_variant == 1, "gg_set_tuning: sweep_variant must be 0 or 1");
+  Tuning& T = S->tune;
+  T.predict_threads = t->predict_threads;
+  T.apply_threads = t->apply_threads;
+  T.finalize_threads = t->finalize_threads;
+  T.keep_threads = t->keep_threads;
+  T.build_blocks_per_sm = t->build_blocks_per_sm;
+  T.sweep_variant = t->sweep_variant;
+  return GG_OK;
+  GG_GUARD_END
+}

@@ -9,7 +9,6 @@
 #include <cmath>
 
 #include "common.cuh"
-#include "warp_union.cuh"
 
 namespace gg {
 
@@ -140,76 +139,19 @@ __global__ void __launch_bounds__(256, 6) k_surface(Grid g, int n, const float4*
   surface[i] = vote ? 0 : 1;
 }
 
-// Warp-cooperative form of k_surface (same sums, same order).
-template <int MM>
-__global__ void __launch_bounds__(256) k_surface_warp(Grid g, int n, const float4* __restrict__ pos,
-                                                      const float* __restrict__ rs,
-                                                      const int32_t* __restrict__ cs, int32_t* __restrict__ surface,
-                                                      float cone, int min_nb) {
-  __shared__ float4 s_p[8][32];
-  __shared__ float s_r[8][32];
-  const int w = threadIdx.x >> 5;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const bool valid = i < n;
-  float3 xi = make_float3(0.f, 0.f, 0.f);
-  float ri = 0.f;
-  int3 q = make_int3(0, 0, 0);
-  if (valid) {
-    xi = f3(pos[i]);
-    ri = rs[i];
-    q = trunc_cell(g, xi);
-  }
-  auto stage = [&](int j, int slot, bool ok) {
-    if (ok) {
-      s_p[w][slot] = pos[j];
-      s_r[w][slot] = rs[j];
-    }
-  };
-  float3 cv = make_float3(0.f, 0.f, 0.f);
-  warp_union_visit(g, cs, valid, q, 7u, 7u, 7u, stage, [&](int j, int k) {
-    if (j == i) return;
-    const float3 d = sub3(xi, f3(s_p[w][k]));
-    const float dis = len3(d);
-    if (dis > 2.0f * (ri + s_r[w][k])) return;
-    cv = add3(cv, m_normalize3<MM>(d));
-  });
-  const float3 c = m_normalize3<MM>(cv);
-  bool vote = false;
-  unsigned nn = 0;
-  warp_union_visit(g, cs, valid, q, 7u, 7u, 7u, stage, [&](int j, int k) {
-    if (j == i) return;
-    float3 b = sub3(f3(s_p[w][k]), xi);
-    const float dis = len3(b);
-    if (dis > 2.0f * (ri + s_r[w][k])) return;
-    // the vote is an OR: once set, later angles cannot change it
-    if (!vote) {
-      b = m_normalize3<MM>(b);
-      if (m_acos<MM>(dot3(b, c)) <= cone) vote = true;
-    }
-    ++nn;
-  });
-  if (valid) surface[i] = (nn <= (unsigned)min_nb || !vote) ? 1 : 0;
-}
-
 void merge_cuts(const gg_system* S, float& f_out, float& T_out);
 
 gg_status surface(gg_system* S, cudaStream_t st) {
   if (S->n <= 0) return GG_OK;
   const int c = S->g.cur;
   prof_begin(S, PC_SURFACE, st);
-  if (S->P.reserved[1] != 1) {
-    auto kern = S->P.math_mode ? k_surface<1> : k_surface<0>;
-    float merge_f = 0.0f, merge_cut = 0.0f;
-    merge_cuts(S, merge_f, merge_cut);
-    kern<<<blocks_for(S->n, 256), 256, 0, st>>>(S->grid, (int)S->n, S->g.pos[c], S->g.rs[c], S->g.cell_start,
-                                                 S->g.surface, S->P.surface_cone, std::cos(S->P.surface_cone),
-                                                 S->P.surface_min_neighbors, &S->scal->rmax_bits, S->g.mass[c],
-                                                 merge_cut, S->g.ld_sum, S->g.ld_cnt);
-  } else {
-    auto kern = S->P.math_mode ? k_surface_warp<1> : k_surface_warp<0>;
-    kern<<<blocks_for(S->n, 256), 256, 0, st>>>(S->grid, (int)S->n, S->g.pos[c], S->g.rs[c], S->g.cell_start,
-                                                 S->g.surface, S->P.surface_cone, S->P.surface_min_neighbors);
-  }
+  auto kern = S->P.math_mode ? k_surface<1> : k_surface<0>;
+  float merge_f = 0.0f, merge_cut = 0.0f;
+  merge_cuts(S, merge_f, merge_cut);
+  kern<<<blocks_for(S->n, 256), 256, 0, st>>>(S->grid, (int)S->n, S->g.pos[c], S->g.rs[c], S->g.cell_start,
+                                               S->g.surface, S->P.surface_cone, std::cos(S->P.surface_cone),
+                                               S->P.surface_min_neighbors, &S->scal->rmax_bits, S->g.mass[c],
+                                               merge_cut, S->g.ld_sum, S->g.ld_cnt);
   count_launches(S, 1);
   prof_end(S, PC_SURFACE, S->n, st);
   GG_CUDA(cudaGetLastError());
@@ -257,56 +199,16 @@ __global__ void __launch_bounds__(256) k_surfdist(Grid g, int n, const float4* _
   sdist[i] = best;
 }
 
-__global__ void __launch_bounds__(256) k_surfdist_warp(Grid g, int n, const float4* __restrict__ pos,
-                                                       const int32_t* __restrict__ surface,
-                                                       const int32_t* __restrict__ cs, float* __restrict__ sdist,
-                                                       float none) {
-  __shared__ float4 s_p[8][32];
-  __shared__ int s_s[8][32];
-  const int w = threadIdx.x >> 5;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const bool valid = i < n;
-  const bool on_surface = valid && surface[i] == 1;
-  float3 xi = make_float3(0.f, 0.f, 0.f);
-  int3 q = make_int3(0, 0, 0);
-  if (valid) {
-    xi = f3(pos[i]);
-    q = trunc_cell(g, xi);
-  }
-  float best = none;
-  warp_union_visit(
-      g, cs, valid && !on_surface, q, 7u, 7u, 7u,
-      [&](int j, int slot, bool ok) {
-        if (ok) {
-          s_p[w][slot] = pos[j];
-          s_s[w][slot] = surface[j];
-        }
-      },
-      [&](int j, int k) {
-        if (j == i || s_s[w][k] == 0) return;
-        const float3 d = sub3(xi, f3(s_p[w][k]));
-        const float d2 = dot3(d, d);
-        if (d2 < best) best = d2;
-      });
-  if (valid) sdist[i] = on_surface ? 0.0f : best;
-}
-
 gg_status surface_distance(gg_system* S, cudaStream_t st) {
   if (S->n <= 0) return GG_OK;
   prof_begin(S, PC_SURFDIST, st);
-  if (S->P.reserved[1] != 1) {
-    GG_CUDA(cudaMemsetAsync(S->g.cell_surf, 0, (size_t)S->grid.C + 1, st));
-    k_mark_surface_cells<<<blocks_for(S->n, 256), 256, 0, st>>>((int)S->n, S->grid.C, S->g.surface, S->g.keys,
-                                                                S->g.cell_surf);
-    k_surfdist<<<blocks_for(S->n, 256), 256, 0, st>>>(S->grid, (int)S->n, S->g.pos[S->g.cur], S->g.surface,
-                                                      S->g.cell_start, S->g.cell_surf, S->g.sdist,
-                                                      S->P.no_surface_distance);
-    count_launches(S, 2);
-  } else {
-    k_surfdist_warp<<<blocks_for(S->n, 256), 256, 0, st>>>(S->grid, (int)S->n, S->g.pos[S->g.cur], S->g.surface,
-                                                           S->g.cell_start, S->g.sdist, S->P.no_surface_distance);
-    count_launches(S, 1);
-  }
+  GG_CUDA(cudaMemsetAsync(S->g.cell_surf, 0, (size_t)S->grid.C + 1, st));
+  k_mark_surface_cells<<<blocks_for(S->n, 256), 256, 0, st>>>((int)S->n, S->grid.C, S->g.surface, S->g.keys,
+                                                              S->g.cell_surf);
+  k_surfdist<<<blocks_for(S->n, 256), 256, 0, st>>>(S->grid, (int)S->n, S->g.pos[S->g.cur], S->g.surface,
+                                                    S->g.cell_start, S->g.cell_surf, S->g.sdist,
+                                                    S->P.no_surface_distance);
+  count_launches(S, 2);
   prof_end(S, PC_SURFDIST, S->n, st);
   GG_CUDA(cudaGetLastError());
   return GG_OK;
@@ -406,62 +308,6 @@ __global__ void __launch_bounds__(256) k_merge_scan(MergeArgs a) {
   }
 }
 
-__global__ void __launch_bounds__(256) k_merge_scan_warp(MergeArgs a) {
-  __shared__ float4 s_p[8][32];
-  __shared__ float s_m[8][32];
-  __shared__ int s_f[8][32];  // remove != 0 or surface != 0
-  const int w = threadIdx.x >> 5;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const bool valid = i < a.n;
-  float mi = 0.f;
-  bool elig = false;
-  if (valid) {
-    a.winner[i] = 0x7fffffff;
-    a.prop[i] = -1;
-    mi = a.mass[i];
-    elig = !(a.surface[i] != 0 || a.remove[i] != 0 || mi < a.min_mass || mi >= a.max_mass || a.sdist[i] < a.sdt);
-  }
-  float3 xi = make_float3(0.f, 0.f, 0.f);
-  int3 q = make_int3(0, 0, 0);
-  if (elig) {
-    xi = f3(a.pos[i]);
-    q = trunc_cell(a.g, xi);
-  }
-  const bool sd_bug = elig && a.sdist[i] < a.sdt;  // Solver.cu:578 tests [i]: always false here
-  float closest = 1000.0f;
-  int ci = -1;
-  float ld = 0.0f;
-  int lc = 0;
-  warp_union_visit(
-      a.g, a.cs, elig, q, 7u, 7u, 7u,
-      [&](int j, int slot, bool ok) {
-        if (ok) {
-          s_p[w][slot] = a.pos[j];
-          s_m[w][slot] = a.mass[j];
-          s_f[w][slot] = (a.remove[j] != 0 || a.surface[j] != 0) ? 1 : 0;
-        }
-      },
-      [&](int j, int k) {
-        if (j >= a.n) return;
-        const float dis = len3(sub3(xi, f3(s_p[w][k])));
-        const bool inr = dis < a.merge_radius_f;
-        if (inr) {
-          ld += s_m[w][k];
-          ++lc;
-        }
-        if (j <= i || s_f[w][k] || sd_bug) return;
-        if (mi + s_m[w][k] > a.max_mass) return;
-        if (inr && dis < closest) {
-          closest = dis;
-          ci = j;
-        }
-      });
-  if (elig && lc > 0 && ci != -1) {
-    a.prop[i] = ci;
-    a.ldens[i] = ld / (float)lc;
-  }
-}
-
 __device__ __forceinline__ bool outer_ok(const MergeArgs& a, int i) {
   return a.surface[i] == 0 && a.sdist[i] > a.sdt;
 }
@@ -555,14 +401,12 @@ gg_status merge_mark(gg_system* S, cudaStream_t st) {
   a.target_density = S->P.target_density;
   a.merge_radius = S->P.merge_radius;
   merge_cuts(S, a.merge_radius_f, a.merge_r2_cut);
-  // the one-thread scan takes the density sums of the surface pass, which
-  // runs the same variant switch
-  a.ld_sum = S->P.reserved[1] != 1 ? S->g.ld_sum : nullptr;
-  a.ld_cnt = S->P.reserved[1] != 1 ? S->g.ld_cnt : nullptr;
+  // the density sums of the surface pass (count -1 where it did not take them)
+  a.ld_sum = S->g.ld_sum;
+  a.ld_cnt = S->g.ld_cnt;
   const int nb = blocks_for(S->n, 256);
   prof_begin(S, PC_MERGE, st);
-  if (S->P.reserved[1] != 1) k_merge_scan<<<nb, 256, 0, st>>>(a);
-  else k_merge_scan_warp<<<nb, 256, 0, st>>>(a);
+  k_merge_scan<<<nb, 256, 0, st>>>(a);
   k_merge_winner<<<nb, 256, 0, st>>>(a);
   k_merge_apply<<<nb, 256, 0, st>>>(a);
   count_launches(S, 3);

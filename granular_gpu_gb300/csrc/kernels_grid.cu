@@ -482,6 +482,16 @@ __global__ void k_hash3(Grid g, const float* __restrict__ pos3, int n, uint32_t*
 }
 
 namespace {
+// Saves the calling thread's current device and restores it on scope exit.
+struct DeviceGuard {
+  int saved = 0;
+  cudaError_t status;
+  DeviceGuard() { status = cudaGetDevice(&saved); }
+  ~DeviceGuard() {
+    if (status == cudaSuccess) cudaSetDevice(saved);
+  }
+};
+
 constexpr int kNoAllocMaxDevices = 64;
 std::mutex g_noalloc_mu;
 uint32_t* g_noalloc_dev[kNoAllocMaxDevices] = {};
@@ -528,6 +538,9 @@ extern "C" gg_status gg_grid_build_noalloc(int32_t device, const float* d_pos, i
                 "use gg_grid_create/gg_grid_build for larger inputs");
       return GG_ERR_CAPACITY;
     }
+    // the caller's current device is put back on every return path
+    DeviceGuard guard;
+    if (guard.status != cudaSuccess) return cuda_status(guard.status, "gg_grid_build_noalloc: cudaGetDevice");
     GG_CUDA(cudaSetDevice(device));
     uint32_t* base = nullptr;
     gg_status rc = noalloc_scratch(device, &base);

@@ -7,7 +7,6 @@
 // one apply kernel with no fill kernels; final_update (:193-270) and the
 // adaptive_last_step fill (:103-108) become one finalize kernel.
 #include "common.cuh"
-#include "warp_union.cuh"
 
 namespace gg {
 
@@ -328,99 +327,6 @@ __global__ void __launch_bounds__(256, 6) k_upsample(UpArgs a) {
   a.upos[i] = make_float4(up.x, up.y, up.z, p4.w);
 }
 
-// Warp-cooperative form of k_upsample (same sums, same order).
-__global__ void __launch_bounds__(256) k_upsample_warp(UpArgs a) {
-  __shared__ float4 s_x[8][32];
-  __shared__ float4 s_v[8][32];
-  const int w = threadIdx.x >> 5;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const bool valid = i < a.n;
-  const Grid g = a.g;
-  float4 p4 = make_float4(0.f, 0.f, 0.f, 0.f);
-  if (valid) p4 = a.upos[i];
-  const float3 p = f3(p4);
-  const int3 q = floor_cell(g, p);
-  float3 wv = make_float3(0.f, 0.f, 0.f), rep = make_float3(0.f, 0.f, 0.f);
-  float gw = 0.f, maxw = 0.f;
-  bool near_b = false;
-  warp_union_visit(
-      g, a.cs, valid, q, 7u, 7u, 7u,
-      [&](int j, int slot, bool ok) {
-        if (ok) {
-          s_x[w][slot] = a.gpos[j];
-          s_v[w][slot] = a.gvel[j];
-        }
-      },
-      [&](int j, int k) {
-        const float4 xj = s_x[w][k];
-        const float3 d = make_float3(p.x - xj.x, p.y - xj.y, p.z - xj.z);
-        const float dd = dot3(d, d);
-        if (dd > a.cut2) return;
-        const float dis = sqrtf(dd);
-        const float t1 = 1.0f - (dis * dis * a.r9);
-        const float wgt = fmaxf(0.0f, t1 * t1 * t1);
-        gw += wgt;
-        const float4 vj = s_v[w][k];
-        wv = add3(wv, smul3(wgt, make_float3(vj.x, vj.y, vj.z)));
-        maxw = fmaxf(maxw, wgt);
-      });
-  warp_union_visit(
-      g, a.bcs, valid, q, 7u, 7u, 7u,
-      [&](int j, int slot, bool ok) {
-        if (ok) s_x[w][slot] = a.bpos[j];
-      },
-      [&](int j, int k) {
-        const float4 b = s_x[w][k];
-        const float3 tb = make_float3(p.x - b.x, p.y - b.y, p.z - b.z);
-        const float dd = dot3(tb, tb);
-        if (dd > a.brad_cut2) return;
-        const float dis = sqrtf(dd);
-        if (dis < a.brad) {
-          near_b = true;
-          const float3 nrm = div3s(tb, dis + 1e-6f);
-          const float force = a.repulsion * (a.brad - dis) / a.brad;
-          rep = add3(rep, mul3s(nrm, force));
-        }
-      });
-  if (!valid) return;
-  const float4 uv4 = a.uvel[i];
-  const float3 uv = f3(uv4);
-  const float3 gdt = make_float3(0.0f * a.dtu, a.gdt_y, 0.0f * a.dtu);
-  float3 nv;
-  if (gw > 1e-6f) {
-    wv = div3s(wv, gw);
-    const float alpha = fmaxf(0.0f, 1.0f - maxw);
-    nv = add3(smul3(alpha, add3(uv, gdt)), smul3(1.0f - alpha, wv));
-  } else {
-    nv = add3(uv, gdt);
-    if (near_b) {
-      nv = mul3s(nv, a.bdamp);
-      if (p.y < a.band) nv.y = nv.y * a.gdamp;
-    }
-  }
-  nv = add3(nv, rep);
-  nv.x = fmaxf(-a.vmax, fminf(nv.x, a.vmax));
-  nv.y = fmaxf(-a.vmax, fminf(nv.y, a.vmax));
-  nv.z = fmaxf(-a.vmax, fminf(nv.z, a.vmax));
-  if (isnan(nv.x) || isnan(nv.y) || isnan(nv.z)) nv = make_float3(0.f, 0.f, 0.f);
-  float3 up = add3(p, mul3s(nv, a.dtu));
-  if (up.y < a.floor_y) {
-    up.y = a.floor_y;
-    nv.y = 0.0f;
-    nv.x = nv.x * a.floor_fric;
-    nv.z = nv.z * a.floor_fric;
-  }
-  if (up.x < 0.0f) {
-    up.x = 0.0f;
-    nv.x = 0.0f;
-  }
-  if (up.z < 0.0f) {
-    up.z = 0.0f;
-    nv.z = 0.0f;
-  }
-  a.uvel[i] = make_float4(nv.x, nv.y, nv.z, 0.f);
-  a.upos[i] = make_float4(up.x, up.y, up.z, p4.w);
-}
 
 gg_status upsample(gg_system* S, cudaStream_t st) {
   if (S->nu <= 0) return GG_OK;
@@ -449,8 +355,7 @@ gg_status upsample(gg_system* S, cudaStream_t st) {
   a.band = S->P.up_ground_band;
   a.gdamp = S->P.up_ground_damping;
   prof_begin(S, PC_UPSAMPLE, st);
-  if (S->P.reserved[1] != 1) k_upsample<<<blocks_for(S->nu, 256), 256, 0, st>>>(a);
-  else k_upsample_warp<<<blocks_for(S->nu, 256), 256, 0, st>>>(a);
+  k_upsample<<<blocks_for(S->nu, 256), 256, 0, st>>>(a);
   count_launches(S, 1);
   prof_end(S, PC_UPSAMPLE, S->nu, st);
   GG_CUDA(cudaGetLastError());

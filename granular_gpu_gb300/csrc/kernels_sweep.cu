@@ -1,6 +1,6 @@
 // kernels_sweep.cu — the Jacobi contact sweep (compute_delta_pos,
 // Solver.cu:361-401, with boundary_constraint :272-307 and
-// particles_constraint :309-359), race-free, with a shared-memory tile.
+// particles_constraint :309-359), race-free.
 //
 // Semantics.  The reference's scatters into delta_pos[j] are overwritten by
 // each thread's final `delta_pos[i] = dp` when the whole grid is resident,
@@ -18,13 +18,10 @@
 // the largest displacement since binning) are skipped; they contribute
 // nothing, so the sum and its order are unchanged.
 //
-// Tiling.  Particles are sorted by cell, so a block of consecutive particles
-// covers a short z-run of one or two (x, y) columns.  The union of their
-// (pruned) stencils is a few columns x a short z-range; each is one
-// contiguous index range of the sorted arrays.  The block copies those
-// ranges (x*, radius, inverse mass) and the cell start offsets into shared
-// memory once, then every thread runs its reference loop from shared memory.
-// Blocks whose union does not fit take the same loop over global memory.
+// Kernels.  The default keeps per-particle contact lists across the sweeps
+// of a substep (k_sweep_nlist_build / k_sweep_nlist_keep); without lists,
+// k_sweep_list scans the 27 cells; k_sweep is the pruned one-thread-per-
+// particle scan the autotuner may pick where lists do not pay.
 #include <algorithm>
 #include <climits>
 
@@ -299,148 +296,6 @@ __global__ void __launch_bounds__(256) k_sweep(SweepArgs a) {
   sweep_global<MM>(a, i, t);
 }
 
-// ------------------------------------------------------------ tiled sweep
-
-constexpr int kTileT = 128;     // particles per block
-constexpr int kTileCap = 1536;  // candidates held in shared memory
-constexpr int kTileZ = 62;      // max cells per column z-run
-constexpr int kCols = 25;       // 5 x 5 column slots around the block
-
-template <int MM>
-__global__ void __launch_bounds__(kTileT) k_sweep_tiled(SweepArgs a) {
-  __shared__ float4 s_x[kTileCap];
-  __shared__ float s_inv[kTileCap];
-  __shared__ int s_cs[kCols][kTileZ + 1];
-  __shared__ int s_zlo[kCols], s_zhi[kCols], s_idx[kCols], s_off[kCols], s_cnt[kCols];
-  __shared__ int s_bx0, s_bx1, s_by0, s_by1, s_ok;
-
-  const Grid& g = a.g;
-  const int tid = threadIdx.x;
-  const int i = blockIdx.x * kTileT + tid;
-  const bool valid = i < a.n;
-  Target t;
-  if (valid) make_target(a, i, a.xs[i], t);
-  if (tid == 0) {
-    s_bx0 = s_by0 = INT_MAX;
-    s_bx1 = s_by1 = INT_MIN;
-    s_ok = 1;
-  }
-  if (tid < kCols) {
-    s_zlo[tid] = INT_MAX;
-    s_zhi[tid] = INT_MIN;
-  }
-  __syncthreads();
-  if (valid) {
-    atomicMin(&s_bx0, t.q.x);
-    atomicMax(&s_bx1, t.q.x);
-    atomicMin(&s_by0, t.q.y);
-    atomicMax(&s_by1, t.q.y);
-  }
-  __syncthreads();
-  const int bx0 = s_bx0, by0 = s_by0;
-  // the tile covers query cells near the grid only; far-out targets (and a
-  // block spread over more than three columns per axis) take the global loop
-  const bool spread_ok = (long long)s_bx1 - bx0 <= 2 && (long long)s_by1 - by0 <= 2 && bx0 >= -1 &&
-                         s_bx1 <= g.nx && by0 >= -1 && s_by1 <= g.ny;
-  if (spread_ok && valid) {
-    // z-run of each (x, y) column this target visits after pruning
-    int zlo = INT_MAX, zhi = INT_MIN;
-    for (int oz = 0; oz < 3; ++oz)
-      if ((t.pm[2] >> oz) & 1u) {
-        zlo = min(zlo, t.q.z + oz - 1);
-        zhi = max(zhi, t.q.z + oz - 1);
-      }
-    if (zlo <= zhi)
-      for (int ox = 0; ox < 3; ++ox) {
-        if (!((t.pm[0] >> ox) & 1u)) continue;
-        for (int oy = 0; oy < 3; ++oy) {
-          if (!((t.pm[1] >> oy) & 1u)) continue;
-          const int slot = (t.q.x + ox - 1 - (bx0 - 1)) * 5 + (t.q.y + oy - 1 - (by0 - 1));
-          atomicMin(&s_zlo[slot], zlo);
-          atomicMax(&s_zhi[slot], zhi);
-        }
-      }
-  }
-  __syncthreads();
-  if (tid == 0) {
-    int ok = spread_ok ? 1 : 0;
-    int total = 0;
-    for (int s = 0; s < kCols && ok; ++s) {
-      const int cx = bx0 - 1 + s / 5, cy = by0 - 1 + s % 5;
-      int zlo = max(s_zlo[s], 0), zhi = min(s_zhi[s], g.nz - 1);
-      s_cnt[s] = 0;
-      s_off[s] = total;
-      s_idx[s] = 0;
-      if (zlo > zhi || cx < 0 || cx >= g.nx || cy < 0 || cy >= g.ny) {
-        s_zlo[s] = 1;
-        s_zhi[s] = 0;
-        continue;
-      }
-      if (zhi - zlo + 1 > kTileZ) {
-        ok = 0;
-        break;
-      }
-      const int key_lo = (cx * g.ny + cy) * g.nz + zlo;
-      const int lo = a.cs[key_lo], hi = a.cs[key_lo + (zhi - zlo + 1)];
-      s_zlo[s] = zlo;
-      s_zhi[s] = zhi;
-      s_idx[s] = lo;
-      s_cnt[s] = hi - lo;
-      total += hi - lo;
-      if (total > kTileCap) ok = 0;
-    }
-    s_ok = ok;
-  }
-  __syncthreads();
-  if (!s_ok) {
-    if (tid == 0) atomicAdd(&a.scal->tile_fallback, 1u);
-    if (valid) sweep_global<MM>(a, i, t);
-    return;
-  }
-  // stage cell starts and candidates
-  for (int s = 0; s < kCols; ++s) {
-    const int ncell = s_zhi[s] - s_zlo[s] + 1;
-    if (ncell <= 0) continue;
-    const int cx = bx0 - 1 + s / 5, cy = by0 - 1 + s % 5;
-    const int key_lo = (cx * g.ny + cy) * g.nz + s_zlo[s];
-    for (int k = tid; k <= ncell; k += kTileT) s_cs[s][k] = a.cs[key_lo + k];
-    const int base = s_idx[s], off = s_off[s], cnt = s_cnt[s];
-    for (int k = tid; k < cnt; k += kTileT) {
-      s_x[off + k] = a.xs[base + k];
-      s_inv[off + k] = a.inv_m[base + k];
-    }
-  }
-  __syncthreads();
-  if (!valid) return;
-
-  float3 dp = make_float3(0.f, 0.f, 0.f);
-  int c = 0, s_loc = 0;
-  for (int ox = 0; ox < 3; ++ox) {
-    for (int oy = 0; oy < 3; ++oy) {
-      for (int oz = 0; oz < 3; ++oz) {
-        const bool usep = use_cell(t.pm, ox, oy, oz);
-        const bool useb = use_cell(t.bm, ox, oy, oz);
-        if (!usep && !useb) continue;
-        const int cx = t.q.x + ox - 1, cy = t.q.y + oy - 1, cz = t.q.z + oz - 1;
-        const int cell = cell_key(g, cx, cy, cz);
-        if (cell == g.C) continue;
-        if (useb) wall_cell<MM>(a, t, cell, dp, c);
-        if (usep) {
-          const int s = (cx - (bx0 - 1)) * 5 + (cy - (by0 - 1));
-          const int zr = cz - s_zlo[s];
-          const int j0 = s_cs[s][zr], j1 = s_cs[s][zr + 1];
-          const int shift = s_off[s] - s_idx[s];
-          for (int j = j0; j < j1; ++j) {
-            if (j == i) continue;
-            particle_pair<MM>(a, t, j, s_x[j + shift], s_inv, j + shift, dp, c, s_loc);
-          }
-        }
-      }
-    }
-  }
-  a.delta[i] = make_float4(dp.x, dp.y, dp.z, __int_as_float((c & 0xffff) | (s_loc << 16)));
-}
-
 // ------------------------------------------------------------ warp sweep
 //
 // The reference sums a particle's corrections over its 27 cells in the
@@ -464,221 +319,6 @@ __device__ __forceinline__ void process_entry(const SweepArgs& a, const Target& 
     wall_contact<MM>(a, t, a.bpos[-e - 1], dp, c);
   } else {
     particle_pair<MM>(a, t, e, a.xs[e], a.inv_m, e, dp, c, s_loc);
-  }
-}
-
-template <int MM>
-__global__ void __launch_bounds__(kWarpThreads, 2) k_sweep_warp_staged(SweepArgs a) {
-  __shared__ int s_list[kWarpThreads / 32][kWarpList][32];
-  __shared__ float4 s_cand[kWarpThreads / 32][32];
-  const Grid& g = a.g;
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int i = blockIdx.x * kWarpThreads + threadIdx.x;
-  const bool valid = i < a.n;
-  Target t;
-  if (valid) make_target(a, i, a.xs[i], t);
-  float3 dp = make_float3(0.f, 0.f, 0.f);
-  int c = 0, s_loc = 0, cnt = 0;
-  // lane's visited z offsets (particles or walls)
-  const unsigned mz = valid ? (t.pm[2] | t.bm[2]) : 0u;
-  const unsigned mxy0 = valid ? (t.pm[0] | t.bm[0]) : 0u, mxy1 = valid ? (t.pm[1] | t.bm[1]) : 0u;
-  int zoff_lo = 2, zoff_hi = -2;
-  for (int k = 0; k < 3; ++k)
-    if ((mz >> k) & 1u) {
-      zoff_lo = min(zoff_lo, k - 1);
-      zoff_hi = max(zoff_hi, k - 1);
-    }
-
-  auto flush = [&]() {
-    for (int k = 0; k < cnt; ++k) process_entry<MM>(a, t, i, s_list[w][k][lane], dp, c, s_loc);
-    cnt = 0;
-  };
-  auto push = [&](int e) {
-    if (cnt == kWarpList) flush();
-    s_list[w][cnt++][lane] = e;
-  };
-
-  unsigned pending = __ballot_sync(0xffffffffu, valid);
-  while (pending) {
-    const int leader = __ffs(pending) - 1;
-    const int gx = __shfl_sync(0xffffffffu, t.q.x, leader);
-    const int gy = __shfl_sync(0xffffffffu, t.q.y, leader);
-    const bool mine = valid && ((pending >> lane) & 1u) && t.q.x == gx && t.q.y == gy;
-    const unsigned members = __ballot_sync(0xffffffffu, mine);
-    pending &= ~members;
-    for (int ox = 0; ox < 3; ++ox) {
-      for (int oy = 0; oy < 3; ++oy) {
-        const bool colin = mine && ((mxy0 >> ox) & 1u) && ((mxy1 >> oy) & 1u);
-        if (!__any_sync(0xffffffffu, colin)) continue;
-        const long long cxl = (long long)gx + ox - 1, cyl = (long long)gy + oy - 1;
-        if (cxl < 0 || cxl >= g.nx || cyl < 0 || cyl >= g.ny) continue;
-        const int cx = (int)cxl, cy = (int)cyl;
-        int zl = colin ? t.q.z + zoff_lo : INT_MAX;
-        int zh = colin ? t.q.z + zoff_hi : INT_MIN;
-        for (int o = 16; o > 0; o >>= 1) {
-          zl = min(zl, __shfl_xor_sync(0xffffffffu, zl, o));
-          zh = max(zh, __shfl_xor_sync(0xffffffffu, zh, o));
-        }
-        zl = max(zl, 0);
-        zh = min(zh, g.nz - 1);
-        if (zl > zh) continue;
-        const int key0 = (cx * g.ny + cy) * g.nz + zl;
-        // per-cell membership of this lane
-        auto in_p = [&](int cz) {
-          const int oz = cz - t.q.z + 1;
-          return colin && oz >= 0 && oz <= 2 && use_cell(t.pm, ox, oy, oz);
-        };
-        auto walls = [&](int cz) {
-          const int oz = cz - t.q.z + 1;
-          const bool useb = colin && oz >= 0 && oz <= 2 && use_cell(t.bm, ox, oy, oz);
-          if (!__any_sync(0xffffffffu, useb)) return;
-          const int cell = key0 + (cz - zl);
-          const int b1 = a.bcs[cell + 1];
-          for (int b = a.bcs[cell]; b < b1; ++b) {
-            const float4 pb = a.bpos[b];
-            if (useb) {
-              const float bx = t.x.x - pb.x, by = t.x.y - pb.y, bz = t.x.z - pb.z;
-              const float d2 = __fmaf_rn(bx, bx, __fmaf_rn(by, by, __fmul_rn(bz, bz)));
-              if (!(d2 > t.Bcut)) push(-b - 1);
-            }
-          }
-        };
-        // the z-run is one contiguous index range of the sorted particles;
-        // cells are entered in order and their walls come first
-        const int J1 = a.cs[key0 + (zh - zl + 1)];
-        int cz = zl;
-        int cnext = a.cs[key0 + 1];
-        walls(cz);
-        bool inp = in_p(cz);
-        for (int base = a.cs[key0]; base < J1; base += 32) {
-          const int jl = base + lane;
-          if (jl < J1) s_cand[w][lane] = a.xs[jl];
-          __syncwarp();
-          const int m = min(32, J1 - base);
-          for (int k = 0; k < m; ++k) {
-            const int j = base + k;
-            while (j >= cnext) {
-              ++cz;
-              cnext = a.cs[key0 + (cz - zl) + 1];
-              walls(cz);
-              inp = in_p(cz);
-            }
-            if (inp && j != i) {
-              const float4 xj = s_cand[w][k];
-              const float dx = t.x.x - xj.x, dy = t.x.y - xj.y, dz = t.x.z - xj.z;
-              const float rr = t.rc + xj.w;
-              const float d2 = __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmul_rn(dz, dz)));
-              if (!(d2 > rr * rr * 1.0001f)) push(j);
-            }
-          }
-          __syncwarp();
-        }
-        // cells after the last particle of the run may still hold walls
-        while (cz < zh) {
-          ++cz;
-          walls(cz);
-        }
-      }
-    }
-  }
-  if (valid) {
-    flush();
-    a.delta[i] = make_float4(dp.x, dp.y, dp.z, __int_as_float((c & 0xffff) | (s_loc << 16)));
-  }
-}
-
-template <int MM>
-__global__ void __launch_bounds__(kWarpThreads) k_sweep_warp_direct(SweepArgs a) {
-  __shared__ int s_list[kWarpThreads / 32][kWarpList][32];
-  const Grid& g = a.g;
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int i = blockIdx.x * kWarpThreads + threadIdx.x;
-  const bool valid = i < a.n;
-  Target t;
-  if (valid) make_target(a, i, a.xs[i], t);
-  float3 dp = make_float3(0.f, 0.f, 0.f);
-  int c = 0, s_loc = 0, cnt = 0;
-  // lane's visited z offsets (particles or walls)
-  const unsigned mz = valid ? (t.pm[2] | t.bm[2]) : 0u;
-  const unsigned mxy0 = valid ? (t.pm[0] | t.bm[0]) : 0u, mxy1 = valid ? (t.pm[1] | t.bm[1]) : 0u;
-  int zoff_lo = 2, zoff_hi = -2;
-  for (int k = 0; k < 3; ++k)
-    if ((mz >> k) & 1u) {
-      zoff_lo = min(zoff_lo, k - 1);
-      zoff_hi = max(zoff_hi, k - 1);
-    }
-
-  auto flush = [&]() {
-    for (int k = 0; k < cnt; ++k) process_entry<MM>(a, t, i, s_list[w][k][lane], dp, c, s_loc);
-    cnt = 0;
-  };
-  auto push = [&](int e) {
-    if (cnt == kWarpList) flush();
-    s_list[w][cnt++][lane] = e;
-  };
-
-  unsigned pending = __ballot_sync(0xffffffffu, valid);
-  while (pending) {
-    const int leader = __ffs(pending) - 1;
-    const int gx = __shfl_sync(0xffffffffu, t.q.x, leader);
-    const int gy = __shfl_sync(0xffffffffu, t.q.y, leader);
-    const bool mine = valid && ((pending >> lane) & 1u) && t.q.x == gx && t.q.y == gy;
-    const unsigned members = __ballot_sync(0xffffffffu, mine);
-    pending &= ~members;
-    for (int ox = 0; ox < 3; ++ox) {
-      for (int oy = 0; oy < 3; ++oy) {
-        const bool colin = mine && ((mxy0 >> ox) & 1u) && ((mxy1 >> oy) & 1u);
-        if (!__any_sync(0xffffffffu, colin)) continue;
-        const long long cxl = (long long)gx + ox - 1, cyl = (long long)gy + oy - 1;
-        if (cxl < 0 || cxl >= g.nx || cyl < 0 || cyl >= g.ny) continue;
-        const int cx = (int)cxl, cy = (int)cyl;
-        int zl = colin ? t.q.z + zoff_lo : INT_MAX;
-        int zh = colin ? t.q.z + zoff_hi : INT_MIN;
-        for (int o = 16; o > 0; o >>= 1) {
-          zl = min(zl, __shfl_xor_sync(0xffffffffu, zl, o));
-          zh = max(zh, __shfl_xor_sync(0xffffffffu, zh, o));
-        }
-        zl = max(zl, 0);
-        zh = min(zh, g.nz - 1);
-        for (int cz = zl; cz <= zh; ++cz) {
-          const int oz = cz - t.q.z + 1;
-          const bool zin = colin && oz >= 0 && oz <= 2;
-          const bool usep = zin && use_cell(t.pm, ox, oy, oz);
-          const bool useb = zin && use_cell(t.bm, ox, oy, oz);
-          const unsigned anyb = __ballot_sync(0xffffffffu, useb);
-          const unsigned anyp = __ballot_sync(0xffffffffu, usep);
-          if (!(anyb | anyp)) continue;
-          const int cell = (cx * g.ny + cy) * g.nz + cz;
-          if (anyb) {
-            const int b1 = a.bcs[cell + 1];
-            for (int b = a.bcs[cell]; b < b1; ++b) {
-              const float4 pb = a.bpos[b];
-              if (useb) {
-                const float bx = t.x.x - pb.x, by = t.x.y - pb.y, bz = t.x.z - pb.z;
-                const float d2 = __fmaf_rn(bx, bx, __fmaf_rn(by, by, __fmul_rn(bz, bz)));
-                if (!(d2 > t.Bcut)) push(-b - 1);
-              }
-            }
-          }
-          if (anyp) {
-            const int j1 = a.cs[cell + 1];
-            for (int j = a.cs[cell]; j < j1; ++j) {
-              const float4 xj = a.xs[j];
-              if (usep && j != i) {
-                const float dx = t.x.x - xj.x, dy = t.x.y - xj.y, dz = t.x.z - xj.z;
-                const float rr = t.rc + xj.w;
-                const float d2 = __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmul_rn(dz, dz)));
-                if (!(d2 > rr * rr * 1.0001f)) push(j);
-              }
-            }
-          }
-        }
-      }
-    }
-  }
-  if (valid) {
-    flush();
-    a.delta[i] = make_float4(dp.x, dp.y, dp.z, __int_as_float((c & 0xffff) | (s_loc << 16)));
   }
 }
 
@@ -1005,54 +645,28 @@ gg_status sweep(gg_system* S, int it, cudaStream_t st) {
     a.eabs = 2.5e-7f * (1.0f + ext);
   }
   prof_begin(S, PC_SWEEP, st);
-  // reserved[0] selects the sweep variant: 0 (default) contact lists when
-  // they are allocated, else variant 3 (or the variant gg_autotune chose); 1 one thread per particle with
-  // pruning; 2 shared-memory tile; 3 one thread per particle over all 27
-  // cells with a deferred contact list; 4 warp-cooperative with staged
-  // candidates; 5 contact lists (variant 3 without them); 6 warp-cooperative
-  // over the stencil union
-  int variant = S->P.reserved[0];
-  if (variant == 0 && S->tune.sweep_variant != 0) variant = S->tune.sweep_variant;
-  if (variant == 0 || variant == 5) variant = S->g.nl_idx ? 5 : 3;
-  switch (variant) {
-    case 1: {
-      auto kern = S->P.math_mode ? k_sweep<1> : k_sweep<0>;
-      kern<<<blocks_for(S->n, 256), 256, 0, st>>>(a);
-      break;
+  // the sweep kernel: contact lists when they are allocated (the default),
+  // else one thread per particle over all 27 cells with its candidates
+  // listed in order; gg_tuning.sweep_variant = 1 picks the pruned
+  // one-thread-per-particle stencil sweep instead (same results)
+  if (S->tune.sweep_variant == 1) {
+    auto kern = S->P.math_mode ? k_sweep<1> : k_sweep<0>;
+    kern<<<blocks_for(S->n, 256), 256, 0, st>>>(a);
+  } else if (S->g.nl_idx) {
+    auto build = S->P.math_mode ? k_sweep_nlist_build<1> : k_sweep_nlist_build<0>;
+    if (it == 0) {
+      build<<<blocks_for(S->n, kBuildThreads), kBuildThreads, 0, st>>>(a, 0);
+    } else {
+      auto keep = S->P.math_mode ? k_sweep_nlist_keep<1> : k_sweep_nlist_keep<0>;
+      const int tk = S->tune.keep_threads;
+      keep<<<blocks_for(S->n, tk), tk, 0, st>>>(a);
+      const int nb = std::min(blocks_for(S->n, kBuildThreads), S->num_sms * S->tune.build_blocks_per_sm);
+      build<<<nb, kBuildThreads, 0, st>>>(a, 1);
+      count_launches(S, 1);
     }
-    case 2: {
-      auto kern = S->P.math_mode ? k_sweep_tiled<1> : k_sweep_tiled<0>;
-      kern<<<blocks_for(S->n, kTileT), kTileT, 0, st>>>(a);
-      break;
-    }
-    case 4: {
-      auto kern = S->P.math_mode ? k_sweep_warp_staged<1> : k_sweep_warp_staged<0>;
-      kern<<<blocks_for(S->n, kWarpThreads), kWarpThreads, 0, st>>>(a);
-      break;
-    }
-    case 5: {
-      auto build = S->P.math_mode ? k_sweep_nlist_build<1> : k_sweep_nlist_build<0>;
-      if (it == 0) {
-        build<<<blocks_for(S->n, kBuildThreads), kBuildThreads, 0, st>>>(a, 0);
-      } else {
-        auto keep = S->P.math_mode ? k_sweep_nlist_keep<1> : k_sweep_nlist_keep<0>;
-        const int tk = S->tune.keep_threads;
-        keep<<<blocks_for(S->n, tk), tk, 0, st>>>(a);
-        const int nb = std::min(blocks_for(S->n, kBuildThreads), S->num_sms * S->tune.build_blocks_per_sm);
-        build<<<nb, kBuildThreads, 0, st>>>(a, 1);
-        count_launches(S, 1);
-      }
-      break;
-    }
-    case 6: {
-      auto kern = S->P.math_mode ? k_sweep_warp_direct<1> : k_sweep_warp_direct<0>;
-      kern<<<blocks_for(S->n, kWarpThreads), kWarpThreads, 0, st>>>(a);
-      break;
-    }
-    default: {
-      auto kern = S->P.math_mode ? k_sweep_list<1> : k_sweep_list<0>;
-      kern<<<blocks_for(S->n, kWarpThreads), kWarpThreads, 0, st>>>(a);
-    }
+  } else {
+    auto kern = S->P.math_mode ? k_sweep_list<1> : k_sweep_list<0>;
+    kern<<<blocks_for(S->n, kWarpThreads), kWarpThreads, 0, st>>>(a);
   }
   count_launches(S, 1);
   prof_end(S, PC_SWEEP, S->n, st);

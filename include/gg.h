@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define GG_ABI_VERSION 1
+#define GG_ABI_VERSION 2
 
 typedef struct gg_system gg_system;
 typedef struct gg_grid gg_grid;
@@ -142,7 +142,6 @@ typedef struct gg_params {
                                   (GG_FIELD_FEATURES, GG_FIELD_WARM_TARGET: training data).  No
                                   counterpart in the reference. */
   float warm_start_scale;      /* multiplies the predicted correction (default 1) */
-  int32_t reserved[2];         /* testing switches: [0] sweep kernel variant, [1] stencil-kernel variant */
 } gg_params;
 
 /* Arguments of GranularSystem::GranularSystem, GranularSystem.hpp:8-14. */
@@ -379,6 +378,9 @@ void gg_grid_destroy(gg_grid* g);
  *     that first call before any stream capture on that device.
  *   - Work is queued on `stream` (NULL: the legacy default stream) and the
  *     call returns without waiting.
+ *   - The call makes `device` current while it queues the work and puts the
+ *     calling thread's previous current device back before it returns, on
+ *     every path, errors included.
  *   - All calls on a device share the one array: calls whose work overlaps
  *     on the GPU (other streams, other host threads) race and must be
  *     serialised by the caller.
@@ -428,6 +430,13 @@ typedef struct gg_tuning {
  * fastest.  Not in residual mode; call before gg_graph_capture.  Allocates a
  * device copy of the state while it runs. */
 gg_status gg_autotune(gg_system* sys, int32_t substeps, gg_tuning* out);
+/* The launch shapes in use, and setting them directly, for example to apply
+ * shapes an earlier gg_autotune chose on the same workload without timing
+ * again.  Results do not depend on them.  gg_set_tuning checks every field
+ * (threads per block a multiple of 32 in 32..1024, blocks per SM 1..32,
+ * sweep_variant 0 or 1) and ignores trials, ms_default and ms_tuned. */
+gg_status gg_get_tuning(gg_system* sys, gg_tuning* out);
+gg_status gg_set_tuning(gg_system* sys, const gg_tuning* tuning);
 
 /*
  * Learned warm start.  No counterpart in the reference: a 48 -> 64 -> 64 -> 3

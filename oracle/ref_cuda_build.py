@@ -32,7 +32,10 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
-REF_SRC = os.path.join(os.environ.get("GG_REFERENCE_DIR", "/root/reference"), "src")
+# The reference checkout: GG_REFERENCE_DIR when set, else where this
+# container mounts it (absent on the GPU host, which uses the prebuilt files).
+REF_ROOT = os.environ.get("GG_REFERENCE_DIR") or "/root/reference"
+REF_SRC = os.path.join(REF_ROOT, "src")
 CUDA = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA, "bin", "nvcc")
 

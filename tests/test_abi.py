@@ -47,13 +47,11 @@ def test_default_params_match():
     q = abi.default_params()
     for name, _ in abi.gg_params._fields_:
         a, b = getattr(p, name), getattr(q, name)
-        if name == "reserved":
-            assert list(a) == list(b)
-        elif isinstance(a, float):
+        if isinstance(a, float):
             assert C.c_float(a).value == C.c_float(b).value or a == b, name
         else:
             assert a == b, name
-    assert gg.lib().gg_abi_version() == 1
+    assert gg.lib().gg_abi_version() == 2
 
 
 def test_invalid_arguments_are_reported_without_a_gpu():
@@ -92,3 +90,20 @@ def test_invalid_arguments_are_reported_without_a_gpu():
 def test_no_fallback_when_library_missing(tmp_path):
     with pytest.raises(abi.NativeLibraryMissing):
         abi.load_library(str(tmp_path / "libgg.so"))
+
+
+def test_noalloc_grid_build_checks_its_limits_before_touching_a_gpu():
+    """gg_grid_build_noalloc rejects inputs beyond its fixed scratch array
+    (262,144 particles, 2^24 cells) with GG_ERR_CAPACITY before any CUDA
+    call, so this runs without a GPU; the pointers are never dereferenced."""
+    lib = gg.lib()
+    cs = (C.c_int32 * 3)(4097, 4096, 1)  # 2^24 + 4096 cells
+    rc = lib.gg_grid_build_noalloc(0, C.c_void_p(16), 10, cs, C.c_float(0.1),
+                                   C.c_void_p(16), C.c_void_p(16), C.c_void_p(16), None)
+    assert rc == abi.GG_ERR_CAPACITY
+    assert b"16777216" in lib.gg_last_error()
+    cs = (C.c_int32 * 3)(1, 1 << 12, 1 << 12)  # exactly 2^24 cells, one particle too many
+    rc = lib.gg_grid_build_noalloc(0, C.c_void_p(16), (1 << 18) + 1, cs, C.c_float(0.1),
+                                   C.c_void_p(16), C.c_void_p(16), C.c_void_p(16), None)
+    assert rc == abi.GG_ERR_CAPACITY
+    assert b"262144" in lib.gg_last_error()

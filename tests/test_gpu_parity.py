@@ -146,14 +146,17 @@ def test_edge_scenes_match_oracle(name):
             assert np.array_equal(s.read(gg.FIELD_POS, gg.SET_UPSAMPLED), o.read(abi.FIELD_POS, abi.SET_UPSAMPLED))
 
 
-@pytest.mark.parametrize("variant,other", [(0, 0), (1, 1), (2, 0), (3, 0), (4, 1), (6, 0)])
-def test_sweep_variants_bit_exact(variant, other):
-    # sweep variants 0-6 (see kernels_sweep.cu); surface/distance/merge/
-    # upsampling one thread per particle (0) or warp-cooperative (1)
+@pytest.mark.parametrize("variant,lists", [(0, True), (0, False), (1, True)])
+def test_sweep_variants_bit_exact(variant, lists):
+    # the sweep kernels (kernels_sweep.cu): contact lists (default), the
+    # 27-cell listed scan without lists (nlist_skin = 0), and the pruned
+    # one-thread-per-particle scan (gg_tuning.sweep_variant = 1)
     desc = workloads.box_drop(n_side=16, substeps=4, iters=5, adaptive=1, upsample_per=2)
-    desc["params"].reserved[0] = variant
-    desc["params"].reserved[1] = other
+    if not lists:
+        desc["params"].nlist_skin = 0.0
     s, o = _pair(desc)
+    s.set_tuning(sweep_variant=variant)
+    assert s.tuning()["sweep_variant"] == variant
     for k in range(1, 8):
         s.step(1)
         o.step(1)
@@ -165,7 +168,6 @@ def test_listed_sweep_bit_exact(skin):
     # contact lists reused across sweeps; the tiny skin forces rebuilds and
     # the large one overflows the lists (full scans)
     desc = workloads.box_drop(n_side=16, substeps=4, iters=5, adaptive=1, upsample_per=2)
-    desc["params"].reserved[0] = 5
     desc["params"].nlist_skin = skin
     s, o = _pair(desc)
     sweeps = desc["params"].stab_iters + desc["params"].iters
@@ -188,7 +190,6 @@ def test_sweep_column_scene_bit_exact():
     # the benchmark scene's geometry (walls, 2x1x1 box, r = 0.002) at a size
     # the oracle finishes quickly
     desc = workloads.column_collapse(counts=(24, 40, 32), upsample_per=2)
-    desc["params"].reserved[0] = 5
     desc["params"].nlist_skin = 0.4 * 0.002
     s, o = _pair(desc)
     for k in range(1, 5):
