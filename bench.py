@@ -2,15 +2,23 @@
 
 A "step" is one substep of the reference's GranularSystem::step (grid
 build, 3 stabilisation + 4 Jacobi sweeps, finalize, upsampling of 4 render
-points per particle, surface detection and merge/split on the integer
-ledger) over 8,388,608 particles resident in HBM.
+points per particle, surface detection and merge/split up to mass 8) over
+8,388,608 particles resident in HBM, with the reference's length constants
+as compiled into its kernels.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl mine|reference]
 
+The headline window is substeps 40 .. 40+K of the collapse, where the first
+merges complete (a merge blends over 40 substeps) and the particle count
+starts to fall; the K substeps right after the W warm-up substeps are
+reported beside it as `early_window`.
+
 N > 1 runs N independent replicas (one per rank, launched by torchrun); the
-path has no exchange step.  `--impl reference` times the CPU restatement of
-the reference's path (the reference itself is CUDA-only, it has no CPU
-implementation) on a bounded sample of the same workload.
+path has no exchange step.  `--impl reference` times the reference's own
+CUDA kernels (its Solver.cu and GranularSystem.cu compiled unmodified for
+sm_103a with its own device flags, driven by oracle/ref_cuda.py, which
+restates its thrust calls in torch) on the same scene, windows and host
+copies; this library is not loaded in that arm.
 """
 import argparse
 import json
@@ -29,7 +37,9 @@ sys.path.insert(0, ROOT)
 
 METRIC = "particle-substeps/s"
 WORKLOAD = "column collapse 128x256x256 (8,388,608 particles, r=0.002, 2x1x1 box, dt=1/120 x 4 substeps, " \
-           "3+4 sweeps, merge/split to mass 8, 4 render points/particle)"
+           "3+4 sweeps, merge/split to mass 8, 4 render points/particle, the reference's length constants " \
+           "as compiled into its kernels)"
+WINDOW_START = 40  # the headline window starts at this substep (the constructor's is substep 1)
 SAMPLE_COUNTS = (64, 64, 64)
 SAMPLE_NOTE = "64x64x64 sub-lattice (262,144 particles) of the same column scene (same box, grid, walls, " \
               "parameters), one oracle substep per step"
@@ -164,7 +174,7 @@ def cpu_sample(steps: int, warmup: int, fp64: bool = True):
     """Times the oracle (CPU restatement) on the bounded sample."""
     from granular_gpu_gb300 import workloads
     from oracle import oracle as orc
-    desc = workloads.column_collapse(counts=SAMPLE_COUNTS)
+    desc = workloads.column_collapse(counts=SAMPLE_COUNTS, constants="reference")
     o = orc.OracleSystem(desc, fp64=fp64)
     o.step(warmup)
     units = 0
@@ -187,7 +197,7 @@ def fp64_error(device: int) -> dict:
     import granular_gpu_gb300 as gg
     from granular_gpu_gb300 import abi, workloads
     from oracle import oracle as orc
-    desc = workloads.column_collapse(counts=SAMPLE_COUNTS)
+    desc = workloads.column_collapse(counts=SAMPLE_COUNTS, constants="reference")
     s = gg.GranularSystem(**workloads.system_kwargs(desc), device=device)
     o = orc.OracleSystem(desc, fp64=True)
     if s.size() != o.size():
@@ -203,20 +213,126 @@ def fp64_error(device: int) -> dict:
     return out
 
 
+def _line_base(args, world, value, ms, dtype, config):
+    return {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": dtype, "data": "synthetic", "config": config}
+
+
+def _config(desc, counts, world, impl_note):
+    return {"workload": WORKLOAD if counts == (128, 256, 256) else f"column collapse {counts}",
+            "particles": desc["n_particles"], "upsampled": desc["n_upsampled"], "boundary": desc["n_boundary"],
+            "cells": int(np.prod(desc["cell_size"])),
+            "window": f"substeps {WINDOW_START}..{WINDOW_START}+K of the collapse (the first merges complete at "
+                      f"substep 41); the K substeps after the W warm-up substeps are `early_window`",
+            "l2": "inputs larger than L2 (about 1.9 GB of particle state per step)",
+            "parallelism": f"replicas x{world}", "implementation": impl_note}
+
+
 def run_reference(args):
-    rank, world, _ = _dist()
+    """The reference's own CUDA kernels on the headline workload: the same
+    scene, windows and host copies as the library's arm.  This library is
+    never loaded here."""
+    rank, world, local = _dist()
     if rank != 0:
         return 0
-    value, threads, dt = cpu_sample(args.steps, args.warmup)
-    line = {
-        "impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * dt / args.steps,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic", "config": {"workload": WORKLOAD, "sample": SAMPLE_NOTE},
-        "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "port",
-                         "sample": SAMPLE_NOTE},
-        "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-    }
+    import torch
+    from oracle import ref_cuda
+    if not ref_cuda.available():
+        print(json.dumps({"impl": "reference", "unavailable": "the reference's kernels were not compiled "
+                          "(oracle/_ref/ is empty: no reference checkout where build() ran)"}), flush=True)
+        return 0
+    from granular_gpu_gb300 import workloads
+    torch.cuda.set_device(local)
+    counts = tuple(int(c) for c in args.counts.split(","))
+    desc = workloads.column_collapse(counts=counts, seed=42, constants="reference")
+    P = desc["params"]
+    n0, nu = desc["n_particles"], desc["n_upsampled"]
+    k = ref_cuda.RefKernels(fma=True)  # the reference's own device flags
+    r = ref_cuda.RefSystem(k, desc["particles"], np.zeros((n0, 3), np.float32), np.ones(n0, np.float32),
+                           desc["boundary"], desc["upsampled"], np.zeros((nu, 3), np.float32),
+                           cell_size=desc["cell_size"], cell_length=desc["cell_length"], dt=desc["dt"],
+                           gravity=desc["gravity"], density=desc["density"], max_iter=P.iters,
+                           stab_iters=P.stab_iters, adaptive=True, max_mass=P.max_mass)
+    r.step()  # the constructor's step (GranularSystem.cu:62)
+    done = 1
+    for _ in range(args.warmup):
+        r.step()
+        done += 1
+
+    def window(steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        units = 0
+        e0.record()
+        for _ in range(steps):
+            units += r.size()
+            r.step()  # ends with a device synchronisation, as GranularSystem::step does
+        e1.record()
+        torch.cuda.synchronize()
+        return units, e0.elapsed_time(e1)
+
+    eu, ems = window(args.steps)
+    done += args.steps
+    early = {"value": eu / (ems / 1e3), "ms_per_step": ems / args.steps,
+             "substeps": f"{2 + args.warmup}..{1 + args.warmup + args.steps}", "particles_now": r.size()}
+    while done < WINDOW_START - 1:
+        r.step()
+        done += 1
+    sampler = ClockSampler(local)
+    sampler.start()
+    n_before = r.size()
+    units, ms = window(args.steps)
+    clocks = sampler.stop()
+    value = units / (ms / 1e3)
+    removed = sum(x[0] for x in r.stats)
+    split = sum(x[1] for x in r.stats)
+    # end to end: the caller's cudaMemcpy of positions and velocities into the
+    # reference's device arrays before each step and of positions,
+    # velocities and render points out of them after it (main.cu:206-209)
+    def pinned(m):
+        return torch.empty((m, 3), dtype=torch.float32, pin_memory=True)
+    hp, hv, hu = pinned(r.size()), pinned(r.size()), pinned(r.upos.shape[0])
+    hp.copy_(r.pos)
+    hv.copy_(r.vel)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e2e_units = h2d = d2h = 0
+    for _ in range(args.steps):
+        m = r.size()
+        if hp.shape[0] != m:
+            hp, hv = pinned(m), pinned(m)
+            hp.copy_(r.pos)
+            hv.copy_(r.vel)
+        r.pos.copy_(hp, non_blocking=True)
+        r.vel.copy_(hv, non_blocking=True)
+        h2d += 2 * m * 12
+        e2e_units += m
+        r.step()
+        m = r.size()
+        if hp.shape[0] != m:
+            hp, hv = pinned(m), pinned(m)
+        hp.copy_(r.pos, non_blocking=True)
+        hv.copy_(r.vel, non_blocking=True)
+        hu.copy_(r.upos, non_blocking=True)
+        torch.cuda.synchronize()
+        d2h += 2 * m * 12 + hu.shape[0] * 12
+    e2e_s = time.perf_counter() - t0
+    line = _line_base(args, 1, value, ms, "f32", _config(
+        desc, counts, 1, "the reference's Solver.cu and GranularSystem.cu kernels compiled unmodified for sm_103a "
+                         "with its own device flags (oracle/_ref/solver.cubin, gsystem.cubin), launched with its "
+                         "launch shapes by oracle/ref_cuda.py, which restates its thrust calls and host "
+                         "orchestration in torch (no per-step allocation, which favours the reference); "
+                         "max_iter 4 and max_mass 8 as the configuration states (literals 5 and 4 there)"))
+    line["impl"] = "reference"
+    line["early_window"] = early
+    line["window"] = {"particles_start": n_before, "particles_now": r.size(), "merged_total": removed,
+                      "split_total": split}
+    line["e2e"] = {"value": e2e_units / e2e_s, "unit": METRIC, "h2d_bytes_per_step": h2d // max(args.steps, 1),
+                   "d2h_bytes_per_step": d2h // max(args.steps, 1)}
+    line["gpu_launches"] = None  # the reference's kernels, not this library's
+    line["clocks"] = clocks
+    k.close()
     print(json.dumps(line), flush=True)
     return 0
 
@@ -255,6 +371,34 @@ def pile_rate(device: int, steps: int) -> dict:
                         "and timed after 100 substeps"}
 
 
+def scaled_rate(device: int, counts, warmup: int, steps: int) -> dict:
+    """The same column with every length constant scaled by r / 0.01 (a
+    configuration of this library the reference's compiled-in constants
+    cannot run), timed right after the warm-up."""
+    import torch
+    import granular_gpu_gb300 as gg
+    from granular_gpu_gb300 import workloads
+    desc = workloads.column_collapse(counts=counts, seed=42, constants="scaled")
+    s = gg.GranularSystem(**workloads.system_kwargs(desc), device=device)
+    s.step(warmup)
+    s.synchronize()
+    st = torch.cuda.ExternalStream(s.stream, device=device)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    units = 0
+    e0.record(st)
+    for _ in range(steps):
+        units += s.size()
+        s.step(1)
+    e1.record(st)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    s.close()
+    return {"metric": METRIC, "value": units / (ms / 1e3), "ms_per_step": ms / steps, "steps": steps,
+            "substeps": f"{2 + warmup}..{1 + warmup + steps}",
+            "workload": "the headline column with wall reach, merge radius, upsampling support and floor scaled "
+                        "by r / 0.01 and render points advected with the substep's dt"}
+
+
 def run_mine(args):
     import torch
     import granular_gpu_gb300 as gg
@@ -267,42 +411,60 @@ def run_mine(args):
         tdist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     torch.cuda.set_device(local)
     counts = tuple(int(c) for c in args.counts.split(","))
-    desc = workloads.column_collapse(counts=counts, seed=42 + rank)
+    desc = workloads.column_collapse(counts=counts, seed=42 + rank, constants="reference")
     if args.math_mode:
         desc["params"].math_mode = args.math_mode
     if args.nlist_skin is not None:
         desc["params"].nlist_skin = args.nlist_skin * 0.002
     n0 = desc["n_particles"]
-    sysg = gg.GranularSystem(**workloads.system_kwargs(desc), device=local)
+    sysg = gg.GranularSystem(**workloads.system_kwargs(desc), device=local)  # substep 1
     stream = torch.cuda.ExternalStream(sysg.stream, device=local)
+    done = 1
     for _ in range(args.warmup):
         sysg.step(1)
+        done += 1
     sysg.synchronize()
 
     def barrier():
         if dist_on:
             tdist.barrier()
 
-    # ---- device-resident timed region
+    def window(steps):
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        barrier()
+        torch.cuda.synchronize()
+        units = 0
+        ev0.record(stream)
+        for _ in range(steps):
+            units += sysg.size()
+            sysg.step(1)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+        return units, ev0.elapsed_time(ev1)
+
+    # ---- early window: the K substeps after the warm-up
+    eu, ems = window(args.steps)
+    done += args.steps
+    ems_max, eu_total = reduce_over_ranks(ems, eu)
+    early = {"value": eu_total / (ems_max / 1e3), "ms_per_step": ems_max / args.steps,
+             "substeps": f"{2 + args.warmup}..{1 + args.warmup + args.steps}", "particles_now": sysg.size()}
+    while done < WINDOW_START - 1:
+        sysg.step(1)
+        done += 1
+    sysg.synchronize()
+    st0 = sysg.stats()
+
+    # ---- headline window, device-resident
     sampler = ClockSampler(local)
     sampler.start()
-    barrier()
-    torch.cuda.synchronize()
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     sysg.profile_begin()
-    units = 0
-    ev0.record(stream)
-    for _ in range(args.steps):
-        units += sysg.size()
-        sysg.step(1)
-    ev1.record(stream)
-    torch.cuda.synchronize()
-    barrier()
+    units, ms = window(args.steps)
     prof = sysg.profile_end()
     launches = prof.pop("_kernel_launches")
     list_builds = prof.pop("_nlist_rebuilds")
     clocks = sampler.stop()
-    ms = ev0.elapsed_time(ev1)
+    st1 = sysg.stats()
     ms_max, total_units = reduce_over_ranks(ms, units)
     value = total_units / (ms_max / 1000.0)
 
@@ -366,15 +528,9 @@ def run_mine(args):
     total_ms = sum(v["ms"] for v in prof.values())
     shares = {k: round(v["ms"] / total_ms, 4) for k, v in prof.items() if v["launches"]}
 
-    line = {
-        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD if counts == (128, 256, 256) else f"column collapse {counts}",
-                   "particles": n0, "upsampled": desc["n_upsampled"],
-                   "boundary": desc["n_boundary"], "cells": int(np.prod(desc["cell_size"])),
-                   "l2": "inputs larger than L2 (about 1.9 GB of particle state per step)",
-                   "parallelism": f"replicas x{world}"},
+    line = _line_base(args, world, value, ms_max, "f32", _config(
+        desc, counts, world, "this library (granular_gpu_gb300/_build/libgg.so), integer mass ledger"))
+    line.update({
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                      "algorithmic_bytes_per_unit": per_unit, "unit_of_work": unit_name,
@@ -390,7 +546,14 @@ def run_mine(args):
                 "d2h_bytes_per_step": d2h // max(args.steps, 1)},
         "gpu_launches": int(launches),
         "clocks": clocks,
-    }
+        "early_window": early,
+        "window": {"particles_start": st0["n_particles"], "particles_now": st1["n_particles"],
+                   "merged_total": st1["merged_total"], "split_total": st1["split_total"],
+                   "merged_in_window": st1["merged_total"] - st0["merged_total"],
+                   "mass_units_conserved": st1["total_mass_units"] == n0 * (1 << 20)},
+    })
+    if rank == 0 and world == 1 and not args.no_scaled:
+        line["column_scaled_constants"] = scaled_rate(local, counts, args.warmup, args.steps)
     if rank == 0 and world == 1 and not args.no_pile:
         # the adaptive-pile configuration: 262,144 particles of r = 0.005 on the
         # floor of a box with a 30-degree ramp, merge/split to mass 8 on the
@@ -447,6 +610,7 @@ def main():
     ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-pile", action="store_true")
+    ap.add_argument("--no-scaled", action="store_true")
     ap.add_argument("--pile-steps", type=int, default=60)
     ap.add_argument("--batched-frames", type=int, default=10)
     ap.add_argument("--learned-frames", type=int, default=150)
@@ -459,10 +623,14 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.impl == "reference":
+        # only the reference's kernels (prebuilt cubins where no checkout is
+        # present); this library is not built or loaded in this arm
+        from oracle import ref_cuda_build
+        ref_cuda_build.build()
+        return run_reference(args)
     import __graft_entry__
     __graft_entry__.build()
-    if args.impl == "reference":
-        return run_reference(args)
     return run_mine(args)
 
 

@@ -118,6 +118,8 @@ gg_status gg_default_params(gg_params* P) {
   P->max_sweeps = 200;
   P->warm_start = 0;
   P->warm_start_scale = 1.0f;
+  P->merge_cas_lag = 4;
+  P->pad_ = 0;
   return GG_OK;
 }
 
@@ -347,6 +349,7 @@ gg_status gg_set_params(gg_system* S, const gg_params* P) {
     return GG_ERR_NOT_SUPPORTED;
   }
   REQUIRE(P->stab_iters >= 0 && P->iters >= 0 && P->max_sweeps >= 0, "gg_set_params: negative sweep count");
+  REQUIRE(P->merge_cas_lag >= 0 && P->merge_cas_lag <= 65536, "gg_set_params: merge_cas_lag must be in 0..65536");
   S->P = *P;
   return GG_OK;
 }

@@ -49,7 +49,9 @@ struct DevScalars {
   unsigned int pen_bits;       // residual mode: largest penetration (float bits)
   unsigned int pen_count;      // residual mode: contacts (particle pairs counted once per side, walls)
   double pen_sum;              // residual mode: sum of their penetrations
-  int error_word;              // bit0 capacity, bit1 numeric
+  int merge_changed[65];       // merge schedule: iteration m changed a claim status (index m, 1..64)
+  int merge_final;             // merge schedule: iteration whose statuses are final
+  int error_word;              // bit0 capacity, bit1 numeric, bit2 timeout, bit3 merge schedule unresolved
   int n_after;                 // particle count after the adaptive step
   int n_removed;
   int n_split;
@@ -60,7 +62,8 @@ struct DevScalars {
 
 constexpr int kMaxSweeps = 256;  // sweeps per substep (stabilisation + Jacobi)
 
-enum ErrorBits { ERR_CAPACITY = 1, ERR_NUMERIC = 2, ERR_TIMEOUT = 4 };
+enum ErrorBits { ERR_CAPACITY = 1, ERR_NUMERIC = 2, ERR_TIMEOUT = 4, ERR_MERGE_SCHEDULE = 8 };
+constexpr int kMergeMaxIter = 64;  // claim-status iterations of the merge schedule
 
 // Largest element count of a set: launches round counts up to whole tiles
 // of at most 4,096 items and index them with signed 32-bit integers.
@@ -115,6 +118,8 @@ struct Granular {
   int32_t* prop = nullptr;
   float* ldens = nullptr;
   int32_t* winner = nullptr;
+  int32_t* claim_tgt = nullptr;  // merge schedule: the proposing partner a proposer claims first, or -1
+  uint8_t* claimed = nullptr;    // merge schedule: 2 x cap claim statuses (iterations ping-pong)
   int32_t* split_flag = nullptr;
   int32_t* keep_flag = nullptr;
   int32_t* split_slot = nullptr;
@@ -213,6 +218,7 @@ struct gg_system {
   float last_residual_max = 0.0f;     // largest penetration
   int stats_blocks = 0;
   int num_sms = 0;
+  int merge_resolve_blocks = 0;  // co-resident blocks of the cooperative merge-schedule kernel
   float nl_skin = 0.0f;                // contact-list skin in use (0 = lists off)
   int64_t steps = 0;
   int64_t launches = 0;                // kernels launched since create

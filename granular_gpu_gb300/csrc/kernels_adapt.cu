@@ -8,9 +8,13 @@
 // host round trip except the new particle count.
 #include <cmath>
 
+#include <cooperative_groups.h>
+
 #include "common.cuh"
 
 namespace gg {
+
+namespace cg = cooperative_groups;
 
 // ------------------------------------------------------------ surface
 
@@ -69,9 +73,11 @@ __global__ void __launch_bounds__(256, 6) k_surface(Grid g, int n, const float4*
   for_each_stencil_column(g, q, [&](int k0, int nc) {
     const int j1 = cs[k0 + nc];
     for (int c0 = cs[k0]; c0 < j1; c0 += 32) {
-      unsigned mask = surface_chunk_mask(pos, c0, min(32, j1 - c0), i, xi, R2);
+      const int cn = min(32, j1 - c0);
+      unsigned mask = surface_chunk_mask(pos, c0, cn, i, xi, R2);
+      // the particle itself counts once, in the chunk that holds it
       const unsigned self = (unsigned)(i - c0);
-      if (ldc && self < 32u) mask |= 1u << self;
+      if (ldc && self < (unsigned)cn) mask |= 1u << self;
       while (mask) {
         const int j = c0 + __ffs(mask) - 1;
         mask &= mask - 1u;
@@ -239,6 +245,11 @@ struct MergeArgs {
   float merge_r2_cut;    // smallest float whose sqrtf reaches merge_radius_f: dis < it <=> dd < this
   const float* __restrict__ ld_sum;    // density sums of the surface pass, or null
   const int32_t* __restrict__ ld_cnt;
+  int lag;                             // merge_cas_lag, in warps
+  int32_t* __restrict__ claim_tgt;
+  uint8_t* claimed0;                   // claim statuses, iterations ping-pong
+  uint8_t* claimed1;
+  DevScalars* scal;
 };
 
 // merge_mark_gpu (Solver.cu:526-653), scan phase: every thread's neighbour
@@ -312,27 +323,96 @@ __device__ __forceinline__ bool outer_ok(const MergeArgs& a, int i) {
   return a.surface[i] == 0 && a.sdist[i] > a.sdt;
 }
 
-// Second-CAS order: ascending proposer index, so the lowest proposer of a
-// target that is not itself a proposer wins it.
+// The compare-and-swaps of merge_mark_gpu (Solver.cu:608-651) race in the
+// reference.  They run here under one fixed legal schedule: every scan ends
+// before any compare-and-swap; then warps of 32 consecutive threads issue
+// theirs in index order, the lanes of a warp together, warp w's first CAS
+// (remove[i]) at time w and its second CAS (remove[closest]) at time
+// w + lag + 1/2.  So:
+//   - proposer i's claim on t can succeed only if t does not propose or
+//     t's own first CAS is later: warp(i) + lag < warp(t);
+//   - i acts at all (wins its own CAS) only if no proposer that acts has
+//     claimed it first;
+//   - of the proposers that act and can claim t, the lowest index wins.
+// Whether a proposer acts depends on proposers below it only, along chains
+// of claims.  The statuses are found by iterating "acts unless an acting
+// claimer claims it" from "every proposer acts" until nothing changes: on
+// a forest of claims each sweep settles one more level, and levels are few
+// (6 to 8 on lattices of 13,824 and 64,000 particles).
+
+__device__ __forceinline__ bool claim_can_win(const MergeArgs& a, int i, int t) {
+  return a.prop[t] < 0 || (i >> 5) + a.lag < (t >> 5);
+}
+
+// Claims on proposing partners (the only ones that change who acts), and
+// iteration 0's statuses: every proposer acts.
+__global__ void k_merge_claims(MergeArgs a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  const int t = a.prop[i];
+  int e = -1;
+  if (t >= 0 && outer_ok(a, i) && a.prop[t] >= 0 && claim_can_win(a, i, t)) e = t;
+  a.claim_tgt[i] = e;
+  a.claimed0[i] = 0;
+}
+
+// Iterates the claim statuses to their fixed point in one cooperative
+// launch (grid-wide barriers between the passes of an iteration); at most
+// kMergeMaxIter iterations, after which the error word records it.
+__global__ void __launch_bounds__(256) k_merge_resolve(MergeArgs a) {
+  cg::grid_group grid = cg::this_grid();
+  const int stride = gridDim.x * blockDim.x;
+  const int i0 = blockIdx.x * blockDim.x + threadIdx.x;
+  for (int m = 1; m <= kMergeMaxIter; ++m) {
+    const uint8_t* prev = (m & 1) ? a.claimed0 : a.claimed1;
+    uint8_t* cur = (m & 1) ? a.claimed1 : a.claimed0;
+    for (int i = i0; i < a.n; i += stride) cur[i] = 0;
+    grid.sync();
+    for (int i = i0; i < a.n; i += stride) {
+      const int t = a.claim_tgt[i];
+      if (t >= 0 && !prev[i]) cur[t] = 1;
+    }
+    grid.sync();
+    int changed = 0;
+    for (int i = i0; i < a.n; i += stride) changed |= cur[i] != prev[i];
+    changed = __syncthreads_or(changed);
+    if (changed && threadIdx.x == 0) atomicOr(&a.scal->merge_changed[m], 1);
+    grid.sync();
+    if (*((volatile int*)&a.scal->merge_changed[m]) == 0) {
+      if (i0 == 0) a.scal->merge_final = m;
+      return;
+    }
+  }
+  if (i0 == 0) {
+    a.scal->merge_final = kMergeMaxIter;
+    atomicOr(&a.scal->error_word, ERR_MERGE_SCHEDULE);
+  }
+}
+
+__device__ __forceinline__ bool was_claimed(const MergeArgs& a, int i) {
+  return ((a.scal->merge_final & 1) ? a.claimed1 : a.claimed0)[i] != 0;
+}
+
 __global__ void k_merge_winner(MergeArgs a) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
   const int t = a.prop[i];
-  if (t < 0 || !outer_ok(a, i) || a.prop[t] >= 0) return;
+  if (t < 0 || was_claimed(a, i) || !outer_ok(a, i) || !claim_can_win(a, i, t)) return;
   atomicMin(&a.winner[t], i);
 }
 
-// The compare-and-swap stages of merge_mark_gpu (Solver.cu:608-651) under
-// the phase-ordered schedule: every proposer first wins its own CAS; then
-// the second CASes run in ascending index.
+// The outcome of the schedule.  A claimed proposer does nothing (its
+// claimer set its flag); an acting one sets its own flag, keeps it alone
+// when its outer check fails (as the reference does), and merges with its
+// partner when it won the partner and the partner passes the check.
 __global__ void k_merge_apply(MergeArgs a) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
   const int t = a.prop[i];
-  if (t < 0) return;
+  if (t < 0 || was_claimed(a, i)) return;
   a.remove[i] = -1;
   if (!outer_ok(a, i)) return;
-  if (a.prop[t] >= 0 || a.winner[t] != i) {
+  if (a.winner[t] != i) {
     a.remove[i] = 0;
     return;
   }
@@ -404,12 +484,28 @@ gg_status merge_mark(gg_system* S, cudaStream_t st) {
   // the density sums of the surface pass (count -1 where it did not take them)
   a.ld_sum = S->g.ld_sum;
   a.ld_cnt = S->g.ld_cnt;
+  a.lag = S->P.merge_cas_lag;
+  a.claim_tgt = S->g.claim_tgt;
+  a.claimed0 = S->g.claimed;
+  a.claimed1 = S->g.claimed + S->cap;
+  a.scal = S->scal;
+  if (S->merge_resolve_blocks <= 0) {
+    int per_sm = 0;
+    GG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_merge_resolve, 256, 0));
+    S->merge_resolve_blocks = std::max(1, per_sm) * S->num_sms;
+  }
   const int nb = blocks_for(S->n, 256);
   prof_begin(S, PC_MERGE, st);
   k_merge_scan<<<nb, 256, 0, st>>>(a);
+  k_merge_claims<<<nb, 256, 0, st>>>(a);
+  {
+    void* args[] = {&a};
+    const int rb = std::min(S->merge_resolve_blocks, nb);
+    GG_CUDA(cudaLaunchCooperativeKernel((const void*)k_merge_resolve, dim3(rb), dim3(256), args, 0, st));
+  }
   k_merge_winner<<<nb, 256, 0, st>>>(a);
   k_merge_apply<<<nb, 256, 0, st>>>(a);
-  count_launches(S, 3);
+  count_launches(S, 5);
   prof_end(S, PC_MERGE, S->n, st);
   GG_CUDA(cudaGetLastError());
   return GG_OK;

@@ -211,7 +211,7 @@ static void free_all(gg_system* S) {
   }
   void* ptrs[] = {G.merge_vel, G.surface, G.sdist, G.cover, G.xs, G.inv_m, G.delta, G.s_extra, G.contacts,
                   G.ncon, G.keys, G.perm, G.cell_start, G.cell_surf, G.prop, G.ldens, G.winner, G.split_flag, G.keep_flag,
-                  G.split_slot, G.keep_slot, G.child_pos, G.nl_idx, G.nl_meta, G.nl_acc, G.nl_queue, G.cell_inc, G.ld_sum, G.ld_cnt, S->b.pos, S->b.animated, S->b.pos_alt,
+                  G.split_slot, G.keep_slot, G.child_pos, G.nl_idx, G.nl_meta, G.nl_acc, G.nl_queue, G.cell_inc, G.ld_sum, G.ld_cnt, G.claim_tgt, G.claimed, S->b.pos, S->b.animated, S->b.pos_alt,
                   S->b.animated_alt, S->b.keys, S->b.perm, S->b.cell_start, S->u.keys, S->u.perm, S->scal,
                   S->stats_partial, S->stage, S->feat, S->xs0, S->warm_target, S->scene_fcap,
                   S->scene_acc};
@@ -257,6 +257,10 @@ gg_status system_create(const gg_desc* d, gg_system** out) {
   if (d->params.stab_iters < 0 || d->params.iters < 0 || d->params.stab_iters + d->params.iters > 64 ||
       d->params.blend_factor <= 0) {
     set_error("gg_create: iteration counts must be in 0..64 and blend_factor > 0");
+    return GG_ERR_INVALID_ARGUMENT;
+  }
+  if (d->params.merge_cas_lag < 0 || d->params.merge_cas_lag > 65536) {
+    set_error("gg_create: merge_cas_lag must be in 0..65536");
     return GG_ERR_INVALID_ARGUMENT;
   }
   int64_t cap = d->max_particles > 0 ? d->max_particles : 2 * d->n_particles;
@@ -315,6 +319,7 @@ gg_status system_create(const gg_desc* d, gg_system** out) {
   ALLOC(G.cell_start, C1); ALLOC(G.cell_surf, C1); ALLOC(G.prop, cap); ALLOC(G.ldens, cap); ALLOC(G.winner, cap);
   ALLOC(G.split_flag, cap); ALLOC(G.keep_flag, cap); ALLOC(G.split_slot, cap); ALLOC(G.keep_slot, cap);
   ALLOC(G.child_pos, cap); ALLOC(G.ld_sum, cap); ALLOC(G.ld_cnt, cap);
+  ALLOC(G.claim_tgt, cap); ALLOC(G.claimed, 2 * cap);
   // contact lists: a negative skin asks for the automatic one, a tenth of
   // the cell length; zero or NaN turns them off
   S->nl_skin = S->P.nlist_skin < 0.0f ? 0.1f * S->grid.L : S->P.nlist_skin;

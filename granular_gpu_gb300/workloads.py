@@ -114,12 +114,19 @@ def box_drop(n_side=32, seed=42, substeps=4, iters=3, adaptive=0, upsample_per=0
 
 
 def column_collapse(counts=(128, 256, 256), r=0.002, seed=42, substeps=4, iters=4, upsample_per=4,
-                    adaptive=1, skip=False):
+                    adaptive=1, skip=False, constants="scaled"):
     """Column collapse: counts lattice (x, y, z) of unit masses of radius r
     at spacing 1.925r (the 2x1x1 box cannot hold 2^23 spheres at 2r with
     aspect 2), jitter +-0.05r, resting in the -x end of a 2x1x1 box;
     dt = 1/120 split into `substeps`; merge/split up to mass 8 on the exact
-    integer ledger; `upsample_per` render points per particle."""
+    integer ledger; `upsample_per` render points per particle.
+
+    constants="scaled" scales every length constant of the reference by
+    r / 0.01 and advects render points with the substep's dt;
+    constants="reference" keeps them as compiled into the reference's
+    kernels (wall reach 0.01 + max(r, 0.01), merge radius 0.035, upsampling
+    support 0.045 and step 0.002, ...), as the reference's own build runs
+    this scene."""
     L = np.float32(CELL_PER_RADIUS * r)
     space = (2.0, 1.0, 1.0)
     walls, cs = box_walls(space, L)
@@ -127,7 +134,12 @@ def column_collapse(counts=(128, 256, 256), r=0.002, seed=42, substeps=4, iters=
     o = 0.0095 * (r / 0.002)
     p = lattice(counts, s, (o, o, o), 0.05 * r, seed)
     dt = 1.0 / 120.0 / substeps
-    params = scaled_params(r, iters=iters, dt_sub=dt, max_mass=8.0, ledger=1)
+    if constants == "reference":
+        params = scaled_params(REF_RADIUS, iters=iters, dt_sub=None, max_mass=8.0, ledger=1)
+    elif constants == "scaled":
+        params = scaled_params(r, iters=iters, dt_sub=dt, max_mass=8.0, ledger=1)
+    else:
+        raise ValueError(constants)
     params.merge_enabled = 1 if adaptive else 0
     params.upsample_enabled = 1 if upsample_per else 0
     ups = None

@@ -142,6 +142,14 @@ typedef struct gg_params {
                                   (GG_FIELD_FEATURES, GG_FIELD_WARM_TARGET: training data).  No
                                   counterpart in the reference. */
   float warm_start_scale;      /* multiplies the predicted correction (default 1) */
+  int32_t merge_cas_lag;       /* 4      the fixed schedule that replaces the race of merge_mark_gpu's
+                                  compare-and-swaps (Solver.cu:608-651): warps of 32 consecutive
+                                  particles issue them in index order, the lanes of a warp together,
+                                  each warp's second CAS (on its partner) merge_cas_lag warps after its
+                                  first (on itself).  0 lets every warp finish before the next starts;
+                                  larger values merge less.  4 merges about as many pairs as the
+                                  reference's own kernel does on a GB300.  0..65536 */
+  int32_t pad_;
 } gg_params;
 
 /* Arguments of GranularSystem::GranularSystem, GranularSystem.hpp:8-14. */

@@ -6,12 +6,12 @@
  * tests/, in __graft_entry__.smoke() and (as the timed CPU baseline) in
  * bench.py.
  *
- * Parity status: the reference ships no tests, fixtures or golden vectors
- * for this path, and its CUDA build cannot run on this machine (no GPU) nor
- * be shipped to the GPU host (no source may travel; no aarch64 toolchain
- * here).  The restatement is therefore pinned only by hand-derived
- * known-answer cases (tests/golden) and by the reference's recorded run
- * statistics; "parity unpinned" against the reference binary itself.
+ * Parity status: pinned.  The reference ships no tests, fixtures or golden
+ * vectors for this path, so the restatement is checked against the
+ * reference's own kernels, compiled from its sources into cubins
+ * (oracle/ref_cuda_build.py) and run on the GB300 from the same states
+ * (tests/test_ref_cuda.py, tests/test_ref_merge_split.py), and against
+ * hand-derived known answers (tests/golden).
  *
  * Two builds of this one file:
  *   GGO_FP64=0  (libggoracle32.so)  FP32 state.  Every expression follows the
@@ -572,13 +572,19 @@ static inline real mass_of_units(int32_t u) { return (real)((double)u / GGO_UNIT
 /*
  * merge_mark_gpu, Solver.cu:526-653.
  *
- * Schedule ("phase order"): every thread finishes its neighbour scan before
- * any thread reaches its compare-and-swaps; then every thread performs its
- * first CAS on remove[i]; then the second CASes on remove[closest] run in
- * ascending thread order.  Under this schedule
- *   - every proposer i (eligible, closest found) wins its own CAS;
- *   - the second CAS succeeds for the lowest proposer of a target that is
- *     not itself a proposer; every other proposer is released.
+ * Schedule ("warp order with a lag"): every thread finishes its neighbour
+ * scan before any thread reaches its compare-and-swaps; then warps of 32
+ * consecutive threads issue their CASes in index order, the lanes of a warp
+ * together: warp w performs its first CAS (on remove[i]) at time w and its
+ * second CAS (on remove[closest]) at time w + merge_cas_lag + 1/2, lanes in
+ * lane order.  Under this schedule, in ascending index:
+ *   - a proposer i (eligible, closest found) whose own CAS comes after a
+ *     successful claim on it is released without acting;
+ *   - otherwise it wins its own CAS, and its claim on t succeeds if no lower
+ *     proposer claimed t first and t's own first CAS (if t proposes) comes
+ *     later, i.e. warp(i) + lag < warp(t).
+ * All claimers of t are below t, so the ascending loop settles each
+ * winner[t] before t itself is reached.
  */
 static void merge_mark(ggo_sys* s) {
   const gg_params* P = &s->P;
@@ -615,26 +621,22 @@ static void merge_mark(ggo_sys* s) {
       s->ldens[i] = ld / (real)lc;
     }
   }
-  /* second CAS winners: lowest proposer (passing the first check) of a
-   * target that is not a proposer */
+  const int64_t lag = P->merge_cas_lag;
   for (int64_t i = 0; i < n; ++i) s->winner[i] = INT_MAX;
   for (int64_t i = 0; i < n; ++i) {
     const int32_t t = s->prop[i];
     if (t < 0) continue;
+    if (s->winner[i] != INT_MAX) continue; /* claimed before its own CAS */
     if (!(s->surface[i] == 0 && s->sdist[i] > sdt)) continue;
-    if (s->prop[t] >= 0) continue;
-    if ((int32_t)i < s->winner[t]) s->winner[t] = (int32_t)i;
+    if (s->prop[t] >= 0 && (i >> 5) + lag >= ((int64_t)t >> 5)) continue; /* t's own CAS came first */
+    if (s->winner[t] == INT_MAX) s->winner[t] = (int32_t)i;
   }
   for (int64_t i = 0; i < n; ++i) {
     const int32_t t = s->prop[i];
-    if (t < 0) continue;
+    if (t < 0 || s->winner[i] != INT_MAX) continue;
     s->remove[i] = -1; /* first CAS */
-  }
-  for (int64_t i = 0; i < n; ++i) {
-    const int32_t t = s->prop[i];
-    if (t < 0) continue;
     if (!(s->surface[i] == 0 && s->sdist[i] > sdt)) continue; /* stays -1 */
-    if (s->prop[t] >= 0 || s->winner[t] != (int32_t)i) { s->remove[i] = 0; continue; }
+    if (s->winner[t] != (int32_t)i) { s->remove[i] = 0; continue; }
     s->remove[t] = -1; /* second CAS */
     if (!(s->surface[t] == 0 && s->sdist[t] > sdt)) { s->remove[i] = 0; continue; }
     const real mi = s->mass[i], mt = s->mass[t];
@@ -848,6 +850,7 @@ void GGO_SYM(default_params)(gg_params* P) {
   P->up_floor_y = 0.04f; P->up_floor_friction = 0.95f; P->up_boundary_damping = 0.8f;
   P->up_ground_band = 0.1f; P->up_ground_damping = 0.5f;
   P->mass_ledger = 0; P->merge_enabled = 1; P->upsample_enabled = 1;
+  P->merge_cas_lag = 4;
 }
 
 ggo_sys* GGO_SYM(create)(const gg_desc* d) {

@@ -1,6 +1,7 @@
 """The reference's own CUDA kernels, driven from Python (TEST INFRASTRUCTURE ONLY).
 
-Only tests/ may import this module.  It loads the cubins that
+Only tests/ and bench.py's reference arm (`--impl reference`, which times
+the reference's own kernels) may import this module.  It loads the cubins that
 `oracle/ref_cuda_build.py` compiled from the reference's `src/Solver.cu` and
 `src/GranularSystem.cu` (unmodified) through the CUDA driver API, launches the
 reference's `__global__` kernels with the reference's launch shapes
@@ -25,6 +26,9 @@ them:
 * `GranularSystem::set_surface_particles` and `find_distance_to_surface`
   (`src/GranularSystem.cu:613-699`) -> `find_cover_vector`, `find_surface`,
   `compute_distance_to_surface`;
+* `Solver::adaptive_sampling` (`src/Solver.cu:856-1242`) -> `merge_mark_gpu`,
+  `merge_count_gpu`, `split_gpu`, `extract_split_particles_kernel`, with the
+  compaction and append of `DArray` / `GranularParticles` restated;
 * `generate_dots` (`src/VBO.hpp:96-106`) -> `generate_dots_CUDA`, the colouring
   of the vertex buffers.
 
@@ -53,6 +57,10 @@ _SIGS = {
     "find_surface": "p p p p i p i3 f f",
     "compute_distance_to_surface": "i p p p i3 f p",
     "generate_dots_CUDA": "p p p i p p f f i p",
+    "merge_mark_gpu": "i p p p p p p p p p p f i3 f p",
+    "merge_count_gpu": "i p p p p p p i p",
+    "split_gpu": "i p p p p p p p p p f i3 p p f f p",
+    "extract_split_particles_kernel": "p p p p i",
 }
 _UNIT_OF = {
     "mapParticles2Cells_CUDA": "solver", "countingInCell_CUDA": "solver",
@@ -60,7 +68,12 @@ _UNIT_OF = {
     "find_cover_vector": "gsystem", "find_surface": "gsystem",
     "compute_distance_to_surface": "gsystem",
     "generate_dots_CUDA": "vbo",
+    "merge_mark_gpu": "solver", "merge_count_gpu": "solver", "split_gpu": "solver",
+    "extract_split_particles_kernel": "solver",
 }
+# struct SplitParticle (Solver.cu:701-706): float3 pos, float3 vel, float mass,
+# bool valid -> 29 bytes, padded to 32 (4-byte alignment)
+SPLIT_PARTICLE_BYTES = 32
 
 
 class _Int3(C.Structure):
@@ -175,14 +188,27 @@ class RefSystem:
 
     State is float3 AoS in device tensors, as the reference keeps it.
     `step()` follows `GranularSystem::step` (`src/GranularSystem.cu:397-453`)
-    for a non-moving boundary: granular and upsampled grid builds,
-    `Solver::step`, `Solver::upsampled_update` and, when `adaptive`, the
-    surface and distance kernels (the merge/split bookkeeping is not
-    driven here).
+    for a non-moving boundary: granular and upsampled grid builds (which
+    permute velocity, mass and the solver's merge, merge-count and remove
+    buffers, `:90-145`), `Solver::step`, `Solver::upsampled_update` and, when
+    `adaptive`, the surface and distance kernels and
+    `Solver::adaptive_sampling` (`src/Solver.cu:856-1242`): `merge_mark_gpu`
+    on every call but the first (`t_merge_iter`, `:36,910-922`; kept per
+    system here, per process there), `merge_count_gpu`, `split_gpu` with its
+    atomic append into a zero-filled SplitParticle buffer, the stable
+    compaction of mass, adaptive_last_step, position, velocity, merge count,
+    merge and remove by `remove == 1` (`DArray::compact`,
+    `src/DArray.hpp:62-113`; merge_velocity is not compacted), and the append
+    of the split children through `extract_split_particles_kernel` with
+    adaptive_last_step 1 and zero solver buffers
+    (`src/GranularParticles.hpp:48-88`).  `max_mass` is the constructor's
+    `_max_mass(4)` (`src/GranularSystem.cu:49`), an argument of the merge and
+    split kernels.
     """
 
     def __init__(self, k: RefKernels, pos, vel, mass, bpos, upos=None, uvel=None, *, cell_size,
-                 cell_length, dt, gravity, density, max_iter=5, stab_iters=3, adaptive=False):
+                 cell_length, dt, gravity, density, max_iter=5, stab_iters=3, adaptive=False,
+                 max_mass=4.0, blend_factor=40):
         torch = k.torch
         self.k, self.t = k, torch
         dev = "cuda"
@@ -202,8 +228,19 @@ class RefSystem:
         self.max_iter = max_iter
         self.stab_iters = stab_iters
         self.adaptive = adaptive
+        self.max_mass = _f32(max_mass)
+        self.blend_factor = int(blend_factor)
         n = self.pos.shape[0]
         self.als = torch.zeros(n, dtype=torch.int32, device=dev)
+        # the solver's buffers (Solver.hpp:108-113), zero-filled like every DArray
+        self.remove = torch.zeros(n, dtype=torch.int32, device=dev)
+        self.merge = torch.zeros(n, dtype=torch.float32, device=dev)
+        self.merge_count = torch.zeros(n, dtype=torch.int32, device=dev)
+        self.merge_vel = torch.zeros((max(n, 1), 3), dtype=torch.float32, device=dev)
+        self.merge_lock = torch.zeros(max(n, 1), dtype=torch.int32, device=dev)
+        self.num_surface = torch.zeros(max(n, 1), dtype=torch.int32, device=dev)
+        self.t_merge_iter = 0
+        self.stats = []  # (removed, split, count before) per adaptive step, Solver.cu:1234-1235
         self.last_n = None
         self.surface = None
         self.surface_distance = None
@@ -215,6 +252,20 @@ class RefSystem:
         (`src/GranularSystem.cu:90-145` gathers every other field), so it
         stays with its array slot."""
         self.als = self.t.as_tensor(np.ascontiguousarray(flags, np.int32), device="cuda").contiguous()
+
+    def set_solver_buffers(self, remove, merge, merge_count, merge_velocity):
+        """Solver::_buffer_remove, _merge, _merge_count, _merge_velocity."""
+        t = self.t
+        self.remove = t.as_tensor(np.ascontiguousarray(remove, np.int32), device="cuda").contiguous()
+        self.merge = t.as_tensor(np.ascontiguousarray(merge, np.float32), device="cuda").contiguous()
+        self.merge_count = t.as_tensor(np.ascontiguousarray(merge_count, np.int32), device="cuda").contiguous()
+        mv = np.ascontiguousarray(merge_velocity, np.float32).reshape(-1, 3)
+        if mv.shape[0] < self.merge_vel.shape[0]:
+            mv = np.concatenate([mv, np.zeros((self.merge_vel.shape[0] - mv.shape[0], 3), np.float32)])
+        self.merge_vel = t.as_tensor(mv, device="cuda").contiguous()
+
+    def size(self) -> int:
+        return int(self.pos.shape[0])
 
     # -- neighbour search (GranularSystem.cu:65-173, 174-280, 282-395)
     def keys(self, pos):
@@ -245,6 +296,9 @@ class RefSystem:
         self.pos, perm, self.cs_g = self.grid(self.pos)
         self.vel = self.vel[perm].contiguous()
         self.mass = self.mass[perm].contiguous()
+        self.merge = self.merge[perm].contiguous()
+        self.merge_count = self.merge_count[perm].contiguous()
+        self.remove = self.remove[perm].contiguous()
         self.perm = perm
         if self.upos is not None and self.upos.shape[0]:
             keys = self.keys(self.upos)
@@ -321,13 +375,65 @@ class RefSystem:
         self.surface = surf[:n]
         self.surface_distance = dist[:n]
 
-    def step(self):
+    # -- Solver::adaptive_sampling (Solver.cu:856-1242)
+    def adaptive_sampling(self):
+        torch = self.t
+        n = self.size()
+        if n == 0:
+            return
+        if self.merge_vel.shape[0] < n:  # the reference's buffer keeps its first length
+            extra = torch.zeros((n - self.merge_vel.shape[0], 3), dtype=torch.float32, device="cuda")
+            self.merge_vel = torch.cat([self.merge_vel, extra]).contiguous()
+            self.merge_lock = torch.zeros(n, dtype=torch.int32, device="cuda")
+            self.num_surface = torch.zeros(n, dtype=torch.int32, device="cuda")
+        if self.t_merge_iter == 1:
+            self.k.launch("merge_mark_gpu", n, n, self.pos, self.mass, self.vel, self.surface,
+                          self.surface_distance, self.num_surface, self.remove, self.merge, self.merge_vel,
+                          self.cs_g, self.max_mass, self.cs, self.L, self.merge_lock)
+            self.t_merge_iter = 0
+        self.t_merge_iter += 1
+        self.k.launch("merge_count_gpu", n, n, self.merge, self.mass, self.vel, self.merge_count, self.remove,
+                      self.merge_vel, self.blend_factor, self.als)
+        splits = torch.zeros(n * SPLIT_PARTICLE_BYTES // 4, dtype=torch.int32, device="cuda")
+        split_count = torch.zeros(1, dtype=torch.int32, device="cuda")
+        self.k.launch("split_gpu", n, n, self.pos, self.mass, self.vel, self.bpos, self.surface, self.remove,
+                      self.merge, self.cs_g, self.cs_b, self.max_mass, self.cs, splits, split_count, self.density,
+                      self.L, self.als)
+        keep = self.remove != 1
+        removed = int(n - int(keep.sum().item()))
+        if removed:
+            self.mass = self.mass[keep].contiguous()
+            self.als = self.als[keep].contiguous()
+            self.pos = self.pos[keep].contiguous()
+            self.vel = self.vel[keep].contiguous()
+            self.merge_count = self.merge_count[keep].contiguous()
+            self.merge = self.merge[keep].contiguous()
+            self.remove = self.remove[keep].contiguous()
+        ns = int(split_count.item())
+        if ns > 0:
+            m_new = torch.zeros(ns, dtype=torch.float32, device="cuda")
+            p_new = torch.zeros((ns, 3), dtype=torch.float32, device="cuda")
+            v_new = torch.zeros((ns, 3), dtype=torch.float32, device="cuda")
+            self.k.launch("extract_split_particles_kernel", ns, splits, m_new, p_new, v_new, ns)
+            self.mass = torch.cat([self.mass, m_new]).contiguous()
+            self.als = torch.cat([self.als, torch.ones(ns, dtype=torch.int32, device="cuda")]).contiguous()
+            self.pos = torch.cat([self.pos, p_new]).contiguous()
+            self.vel = torch.cat([self.vel, v_new]).contiguous()
+            zi = torch.zeros(ns, dtype=torch.int32, device="cuda")
+            self.remove = torch.cat([self.remove, zi]).contiguous()
+            self.merge_count = torch.cat([self.merge_count, zi]).contiguous()
+            self.merge = torch.cat([self.merge, torch.zeros(ns, dtype=torch.float32, device="cuda")]).contiguous()
+        self.stats.append((removed, ns, n))
+
+    def step(self, sync: bool = True):
         self.neighbor_search()
         self.solver_step()
         self.upsampled_update()
         if self.adaptive:
             self.surface_pass()
-        self.k.synchronize()
+            self.adaptive_sampling()
+        if sync:
+            self.k.synchronize()
 
     def read(self, name: str):
         return getattr(self, name).detach().cpu().numpy()

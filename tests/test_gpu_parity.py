@@ -22,7 +22,7 @@ TOL = 1e-5 * R
 
 def _pair(desc, fp64=False, mode=1):
     desc["params"].math_mode = mode
-    s = gg.GranularSystem(**workloads.system_kwargs(desc), device=0)
+    s = gg.GranularSystem(**workloads.system_kwargs(desc), masses=desc.get("masses"), device=0)
     o = orc.OracleSystem(desc, fp64=fp64)
     return s, o
 
@@ -224,16 +224,23 @@ def test_reference_iteration_counts_and_upsampling():
         assert np.array_equal(vg, vo)
 
 
-@pytest.mark.parametrize("ledger", [0, 1])
-def test_adaptive_merge_split_match_oracle(ledger):
+@pytest.mark.parametrize("ledger,mixed", [(0, False), (1, False), (0, True), (1, True)])
+def test_adaptive_merge_split_match_oracle(ledger, mixed):
+    # mixed: masses drawn from 1, 1.5, 2 and 3, so that the merge density
+    # (an average mass) and the merge velocity depend on which neighbours
+    # are summed, and heavy surface particles split
     desc = workloads.box_drop(n_side=14, substeps=4, iters=5, adaptive=1, upsample_per=2)
     desc["params"].mass_ledger = ledger
+    if mixed:
+        rng = np.random.default_rng(9)
+        desc["masses"] = rng.choice(np.array([1.0, 1.0, 1.5, 2.0, 3.0], np.float32), desc["n_particles"])
     s, o = _pair(desc)
     for k in range(1, 56):
         s.step(1)
         o.step(1)
         _compare(s, o, k)
-        for f in (gg.FIELD_REMOVE, gg.FIELD_MERGE_COUNT, gg.FIELD_SURFACE, gg.FIELD_ADAPTIVE_LAST_STEP):
+        for f in (gg.FIELD_REMOVE, gg.FIELD_MERGE_COUNT, gg.FIELD_SURFACE, gg.FIELD_ADAPTIVE_LAST_STEP,
+                  gg.FIELD_MERGE, gg.FIELD_MERGE_VELOCITY):
             a, b = s.read(f), o.read(f)
             assert np.array_equal(a, b), f"step {k}: field {f} differs"
         assert np.array_equal(s.read(gg.FIELD_MASS), o.read(abi.FIELD_MASS)), f"step {k}: masses"
@@ -242,7 +249,9 @@ def test_adaptive_merge_split_match_oracle(ledger):
     st = s.stats()
     assert st["merged_total"] > 0, "scene must merge within 55 steps (first merge completes at step 40)"
     if ledger:
-        assert st["total_mass_units"] == desc["n_particles"] * abi.UNITS_PER_MASS
+        m0 = desc.get("masses")
+        total = desc["n_particles"] if m0 is None else float(np.sum(m0, dtype=np.float64))
+        assert st["total_mass_units"] == round(total * abi.UNITS_PER_MASS)
 
 
 def test_ledger_conserves_mass_exactly_through_merge_and_split():

@@ -196,7 +196,7 @@ def test_surface_kernels_match_reference(kernels):
     s = gg.GranularSystem(**workloads.system_kwargs(desc), device=0)
     checked = blended = 0
     for step in range(1, 92):
-        compare = step in (3, 45, 60, 75, 90)
+        compare = step in (3, 10, 20, 30, 40, 45, 60, 75, 90)
         if compare:
             ref = _ref_from(kernels[False], s, desc, adaptive=True)
             ref.neighbor_search()
