@@ -68,7 +68,7 @@ constexpr int kMergeMaxIter = 64;  // claim-status iterations of the merge sched
 // Largest element count of a set: launches round counts up to whole tiles
 // of at most 4,096 items and index them with signed 32-bit integers.
 constexpr int64_t kMaxCount = ((int64_t)1 << 31) - ((int64_t)1 << 16);
-constexpr int kNlistMax = 32;  // contact candidates kept per particle
+constexpr int kNlistMax = 64;  // contact candidates kept per particle (walls within reach included)
 
 // Kernel classes timed by gg_profile_*.
 enum ProfClass {

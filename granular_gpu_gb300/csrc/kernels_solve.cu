@@ -235,6 +235,13 @@ struct UpArgs {
 // candidate some lane hits.
 // 6 resident blocks of 256 (40 registers, no spills): the kernel is bound by
 // instruction issue, and 48 warps per SM hide its load latency better than 40.
+//
+// ALL: the support reaches every candidate of the stencil (a candidate lies
+// within 2 cell lengths of the point along each axis, so within sqrt(12) L,
+// and the support covers that), as with the reference's radius 0.045 and
+// cells of 0.00808; the candidates are then summed without the mask pass,
+// exactly as the reference does.
+template <bool ALL>
 __global__ void __launch_bounds__(256, 6) k_upsample(UpArgs a) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
@@ -249,28 +256,37 @@ __global__ void __launch_bounds__(256, 6) k_upsample(UpArgs a) {
   // stencil column as one index range (the reference's order within each).
   for_each_stencil_column(g, q, [&](int k0, int nc) {
     const int j1 = a.cs[k0 + nc];
-    for (int c0 = a.cs[k0]; c0 < j1; c0 += 32) {
-      const int cn = min(32, j1 - c0);
-      unsigned mask = 0u;
+    // the reference's weight (Solver.cu:1281-1287) for candidate j
+    auto weigh = [&](int j) {
+      const float4 xj = a.gpos[j];
+      const float3 d = make_float3(p.x - xj.x, p.y - xj.y, p.z - xj.z);
+      const float dis = sqrtf(dot3(d, d));
+      const float t1 = 1.0f - (dis * dis * a.r9);
+      const float w = fmaxf(0.0f, t1 * t1 * t1);
+      gw += w;
+      const float4 vj = a.gvel[j];
+      wv = add3(wv, smul3(w, make_float3(vj.x, vj.y, vj.z)));
+      maxw = fmaxf(maxw, w);
+    };
+    if (ALL) {
+#pragma unroll 2
+      for (int j = a.cs[k0]; j < j1; ++j) weigh(j);
+    } else {
+      for (int c0 = a.cs[k0]; c0 < j1; c0 += 32) {
+        const int cn = min(32, j1 - c0);
+        unsigned mask = 0u;
 #pragma unroll 8
-      for (int b = 0; b < cn; ++b) {
-        const float4 xj = a.gpos[c0 + b];
-        const float dx = p.x - xj.x, dy = p.y - xj.y, dz = p.z - xj.z;
-        const float dd = __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmul_rn(dz, dz)));
-        mask |= (dd <= a.cut2 ? 1u : 0u) << b;
-      }
-      while (mask) {
-        const int j = c0 + __ffs(mask) - 1;
-        mask &= mask - 1u;
-        const float4 xj = a.gpos[j];
-        const float3 d = make_float3(p.x - xj.x, p.y - xj.y, p.z - xj.z);
-        const float dis = sqrtf(dot3(d, d));
-        const float t1 = 1.0f - (dis * dis * a.r9);
-        const float w = fmaxf(0.0f, t1 * t1 * t1);
-        gw += w;
-        const float4 vj = a.gvel[j];
-        wv = add3(wv, smul3(w, make_float3(vj.x, vj.y, vj.z)));
-        maxw = fmaxf(maxw, w);
+        for (int b = 0; b < cn; ++b) {
+          const float4 xj = a.gpos[c0 + b];
+          const float dx = p.x - xj.x, dy = p.y - xj.y, dz = p.z - xj.z;
+          const float dd = __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmul_rn(dz, dz)));
+          mask |= (dd <= a.cut2 ? 1u : 0u) << b;
+        }
+        while (mask) {
+          const int j = c0 + __ffs(mask) - 1;
+          mask &= mask - 1u;
+          weigh(j);
+        }
       }
     }
     const int k1 = a.bcs[k0 + nc];
@@ -354,8 +370,12 @@ gg_status upsample(gg_system* S, cudaStream_t st) {
   a.bdamp = S->P.up_boundary_damping;
   a.band = S->P.up_ground_band;
   a.gdamp = S->P.up_ground_damping;
+  // every candidate of a point's stencil lies within sqrt(12) cell lengths
+  const float reach2 = 12.0f * S->grid.L * S->grid.L * 1.001f;
+  const bool all_in = reach2 * S->P.up_inv_h2 < 0.999f;
   prof_begin(S, PC_UPSAMPLE, st);
-  k_upsample<<<blocks_for(S->nu, 256), 256, 0, st>>>(a);
+  if (all_in) k_upsample<true><<<blocks_for(S->nu, 256), 256, 0, st>>>(a);
+  else k_upsample<false><<<blocks_for(S->nu, 256), 256, 0, st>>>(a);
   count_launches(S, 1);
   prof_end(S, PC_UPSAMPLE, S->nu, st);
   GG_CUDA(cudaGetLastError());

@@ -512,9 +512,9 @@ __global__ void __launch_bounds__(256, 5) k_sweep_nlist_keep(SweepArgs a) {
   }
 }
 
-// List build: scan the 27 cells in the reference order, keep the candidates
-// within reach of the skin (in shared memory, one column per lane), store
-// the list, then run it.  Every particle at the first sweep of a substep;
+// List build: scan the 27 cells in the reference order, write the
+// candidates within reach of the skin to the particle's list as they are
+// found, then run the list.  Every particle at the first sweep of a substep;
 // the queued ones later.
 constexpr int kBuildThreads = 128;
 
@@ -523,9 +523,8 @@ constexpr int kBuildThreads = 128;
 // cost (72 registers and 7 blocks measured 3 % slower over the sweeps).
 template <int MM>
 __global__ void __launch_bounds__(kBuildThreads, 8) k_sweep_nlist_build(SweepArgs a, int queued) {
-  __shared__ int s_list[kBuildThreads / 32][kNlistMax][32];
   const Grid& g = a.g;
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
   const int total = queued ? a.scal->nl_queued[a.it] : a.n;
   for (int base = blockIdx.x * kBuildThreads; base < total; base += gridDim.x * kBuildThreads) {
     const int slot = base + threadIdx.x;
@@ -542,8 +541,9 @@ __global__ void __launch_bounds__(kBuildThreads, 8) k_sweep_nlist_build(SweepArg
     const float Bs2 = Bs * Bs * 1.0001f;
     const float rcs = t.rc + a.skin;
     int cnt = 0;
+    int32_t* __restrict__ li = a.nl_idx + i;
     auto push = [&](int e) {
-      if (cnt < kNlistMax) s_list[w][cnt][lane] = e;
+      if (cnt < kNlistMax) li[(size_t)cnt * a.cap] = e;
       ++cnt;
     };
     // candidates in chunks of 32: a mask of those within the reach of the
@@ -599,12 +599,12 @@ __global__ void __launch_bounds__(kBuildThreads, 8) k_sweep_nlist_build(SweepArg
       sweep_global<MM>(a, i, t);
       continue;
     }
-    for (int k = 0; k < cnt; ++k) a.nl_idx[(size_t)k * a.cap + i] = s_list[w][k][lane];
     a.nl_meta[i] = make_int4(t.q.x, t.q.y, t.q.z, cnt);
     a.nl_acc[i] = 0.0f;
     float3 dp = make_float3(0.f, 0.f, 0.f);
     int c = 0, s_loc = 0;
-    apply_entries<MM>(a, t, cnt, [&](int k) { return s_list[w][k][lane]; }, dp, c, s_loc);
+    // the list this thread just wrote (its own stores: read back in order)
+    apply_entries<MM>(a, t, cnt, [&](int k) { return li[(size_t)k * a.cap]; }, dp, c, s_loc);
     a.delta[i] = make_float4(dp.x, dp.y, dp.z, __int_as_float((c & 0xffff) | (s_loc << 16)));
   }
 }

@@ -126,8 +126,8 @@ typedef struct gg_params {
   float nlist_skin;            /* skin of the per-particle contact lists reused across the sweeps
                                   of a substep: a length; negative (default) = a tenth of the
                                   cell length; 0 = scan the stencil every sweep.  Results do
-                                  not depend on it, only the speed and memory (148 bytes per
-                                  particle of capacity) do. */
+                                  not depend on it, only the speed and memory (276 bytes per
+                                  particle of capacity: 64 candidates and their bookkeeping) do. */
   float target_residual;       /* > 0: after the stabilisation sweeps, Jacobi sweeps run until the
                                   mean penetration over the contacts at x* (particle pairs
                                   r_i + r_j - |x_i - x_j| > 0 and walls), measured before each sweep,
