@@ -568,23 +568,28 @@ def run_mine(args):
         line["batched_scenes"]["unit"] = METRIC
     if rank == 0 and world == 1 and not args.no_learned:
         # learned warm start vs the plain sweeps, to the same residual, on a
-        # held-out scene (device time of whole substeps, CUDA events)
+        # held-out scene (device time of whole substeps, CUDA events): the
+        # residual the configuration names (1e-3 r) and a looser one (1e-2 r)
         from granular_gpu_gb300 import learn
         mlp = learn.load_mlp(device=local)
-        ev = learn.evaluate(mlp, seeds=(101,), frames=args.learned_frames, device=local)
+        runs = {}
+        for tol, frames, cap in ((1e-3, args.learned_frames, 2000), (1e-2, 150, 250)):
+            ev = learn.evaluate(mlp, seeds=(101,), frames=frames, tol=tol, max_sweeps=cap, device=local)
+            sc = ev["scenes"][0]
+            runs[tol] = {
+                "time_ratio": ev["time_ratio"], "sweep_ratio": ev["sweep_ratio"], "target_ratio": 0.6,
+                "plain_ms": ev["plain_ms"], "learned_ms": ev["learned_ms"], "plain_sweeps": ev["plain_sweeps"],
+                "learned_sweeps": ev["learned_sweeps"], "max_sweeps": cap,
+                "plain_capped_frames": sc["plain_capped_frames"], "learned_capped_frames": sc["learned_capped_frames"],
+                "residual": f"mean penetration over contacts <= {tol:g} r, checked before every Jacobi sweep "
+                            f"(cap {cap} sweeps; a capped plain frame stops short, which favours the plain solver)",
+                "scene": f"block 0.6x0.4x0.6 of {sc['particles']} particles (r=0.005, spacing 2r) dropped 0.02 onto "
+                         f"the floor, held-out seed {sc['seed']}, {frames} substeps of 1/240 s"}
         mlp.close()
-        sc = ev["scenes"][0]
-        line["learned_warm_start"] = {
-            "time_ratio": ev["time_ratio"], "sweep_ratio": ev["sweep_ratio"], "target_ratio": 0.6,
-            "plain_ms": ev["plain_ms"], "learned_ms": ev["learned_ms"], "plain_sweeps": ev["plain_sweeps"],
-            "learned_sweeps": ev["learned_sweeps"], "plain_capped_frames": sc["plain_capped_frames"],
-            "learned_capped_frames": sc["learned_capped_frames"],
-            "residual": "mean penetration over contacts <= 1e-2 r, checked before every Jacobi sweep (cap 250); "
-                        "the plain sweeps do not bring the max penetration to 1e-3 r on a pile",
-            "scene": f"block 0.6x0.4x0.6 of {sc['particles']} particles (r=0.005, spacing 2r) dropped 0.02 onto "
-                     f"the floor, held-out seed {sc['seed']}, {args.learned_frames} substeps of 1/240 s",
-            "network": "48-64-64-3 MLP, BF16 tcgen05 kernels, trained on 2,000 solver frames "
-                       "(granular_gpu_gb300/weights/warm_start_mlp.npy)"}
+        line["learned_warm_start"] = dict(runs[1e-3])
+        line["learned_warm_start"]["at_1e-2_r"] = runs[1e-2]
+        line["learned_warm_start"]["network"] = ("48-64-64-3 MLP, BF16 tcgen05 kernels, trained on 2,000 solver frames "
+                                                 "solved to 1e-3 r (granular_gpu_gb300/weights/warm_start_mlp.npy)")
     if rank == 0 and world == 1 and not args.no_cpu:
         cv, threads, _ = cpu_sample(steps=args.cpu_steps, warmup=1)
         line["cpu_baseline"] = {"value": cv, "unit": METRIC, "cores": threads, "kind": "port",
@@ -595,6 +600,41 @@ def run_mine(args):
         print(json.dumps(line), flush=True)
     if dist_on:
         tdist.destroy_process_group()
+    return 0
+
+
+def run_profile_window(args):
+    """Steps the column to the headline window, then runs --steps substeps
+    between cudaProfilerStart and cudaProfilerStop (for `ncu
+    --profile-from-start off`), and prints the library's per-class CUDA-event
+    times of those substeps as one JSON line.  No timing line of the
+    benchmark; a number taken under a profiler is not one."""
+    import torch
+    import granular_gpu_gb300 as gg
+    from granular_gpu_gb300 import workloads
+    counts = tuple(int(c) for c in args.counts.split(","))
+    desc = workloads.column_collapse(counts=counts, seed=42, constants=args.constants)
+    if args.nlist_skin is not None:
+        desc["params"].nlist_skin = args.nlist_skin * 0.002
+    s = gg.GranularSystem(**workloads.system_kwargs(desc), device=0)
+    start = args.window_start if args.window_start is not None else WINDOW_START
+    if start > 1:
+        s.step(start - 1)
+    s.synchronize()
+    torch.cuda.synchronize()
+    s.profile_begin()
+    torch.cuda.profiler.start()
+    n0 = s.size()
+    s.step(args.steps)
+    s.synchronize()
+    torch.cuda.profiler.stop()
+    prof = s.profile_end()
+    out = {"workload": f"column collapse {counts}, {args.constants} constants", "substeps": args.steps,
+           "window_start": start, "particles": n0, "ms_per_substep": {
+               k: round(v["ms"] / args.steps, 4) for k, v in prof.items() if isinstance(v, dict) and v["launches"]},
+           "list_builds": prof.get("_nlist_rebuilds"), "kernel_launches": prof.get("_kernel_launches")}
+    s.close()
+    print(json.dumps(out), flush=True)
     return 0
 
 
@@ -613,14 +653,26 @@ def main():
     ap.add_argument("--no-scaled", action="store_true")
     ap.add_argument("--pile-steps", type=int, default=60)
     ap.add_argument("--batched-frames", type=int, default=10)
-    ap.add_argument("--learned-frames", type=int, default=150)
+    ap.add_argument("--learned-frames", type=int, default=80,
+                    help="substeps of the learned-warm-start comparison at 1e-3 r")
     ap.add_argument("--counts", default="128,256,256",
                     help="column lattice x,y,z (the benchmark workload is 128,256,256)")
     ap.add_argument("--math-mode", type=int, default=0)
     ap.add_argument("--nlist-skin", type=float, default=None,
                     help="contact-list skin in radii of 0.002 (default: a tenth of the cell length; "
                          "0 turns the lists off)")
+    ap.add_argument("--profile-window", action="store_true",
+                    help="profiling driver: step to the window, run --steps substeps between "
+                         "cudaProfilerStart/Stop, print per-class times (no benchmark line)")
+    ap.add_argument("--constants", choices=["reference", "scaled"], default="reference",
+                    help="with --profile-window: the reference's length constants or them scaled by r/0.01")
+    ap.add_argument("--window-start", type=int, default=None,
+                    help="with --profile-window: first profiled substep (default: the headline window's)")
     args = ap.parse_args()
+    if args.profile_window:
+        import __graft_entry__
+        __graft_entry__.build()
+        return run_profile_window(args)
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

@@ -40,12 +40,14 @@ inline UDiv make_udiv(uint32_t d) {
 }
 
 // Scalars that live on the device so a substep needs no host round trip.
+constexpr int kMaxSweeps = 2048;  // sweeps per substep (stabilisation + Jacobi)
+
 struct DevScalars {
   unsigned int rmax_bits;      // max contact radius (float bits), this step
-  unsigned int inc_bits[256];  // per sweep: max |x* increment| (float bits)
+  unsigned int inc_bits[kMaxSweeps];  // per sweep: max |x* increment| (float bits)
   unsigned int disp0_bits;     // max |dt v| of the predict (float bits)
   unsigned int tile_fallback;  // sweep blocks that could not use the shared-memory tile
-  int nl_queued[256];          // per sweep: particles whose contact list is rebuilt
+  int nl_queued[kMaxSweeps];          // per sweep: particles whose contact list is rebuilt
   unsigned int pen_bits;       // residual mode: largest penetration (float bits)
   unsigned int pen_count;      // residual mode: contacts (particle pairs counted once per side, walls)
   double pen_sum;              // residual mode: sum of their penetrations
@@ -60,7 +62,6 @@ struct DevScalars {
   unsigned long long nlist_rebuilds;  // listed-sweep list builds (not reset per substep)
 };
 
-constexpr int kMaxSweeps = 256;  // sweeps per substep (stabilisation + Jacobi)
 
 enum ErrorBits { ERR_CAPACITY = 1, ERR_NUMERIC = 2, ERR_TIMEOUT = 4, ERR_MERGE_SCHEDULE = 8 };
 constexpr int kMergeMaxIter = 64;  // claim-status iterations of the merge schedule

@@ -135,7 +135,7 @@ typedef struct gg_params {
                                   then unused.  0 (default): the fixed `iters` sweeps of the
                                   reference.  No counterpart in the reference. */
   int32_t max_sweeps;          /* cap on the Jacobi sweeps of a substep in residual mode (default 200;
-                                  stab_iters + max_sweeps is capped at 256) */
+                                  stab_iters + max_sweeps is capped at 2048) */
   int32_t warm_start;          /* 0 (default) off; 1 = before the sweeps, add the attached network's
                                   predicted correction to x* (gg_set_warm_start); 2 = record the
                                   features and, after the sweeps, the correction the sweeps reached

@@ -172,10 +172,22 @@ def test_isolated_pairs_match_reference_build(kernels, stab, iters):
     _check_step(kernels, desc)
 
 
-def test_upsampling_kernel_matches_reference(kernels):
-    desc = _box(n_side=10, upsample_per=4)
+@pytest.mark.parametrize("scene", ["box", "column"])
+def test_upsampling_kernel_matches_reference(kernels, scene):
+    # box: r = 0.01, the support 0.045 reaches part of the stencil (masked
+    # scan); column: r = 0.002 with the reference's constants, the support
+    # covers the whole stencil (two points per thread, packed arithmetic)
+    if scene == "box":
+        desc = _box(n_side=10, upsample_per=4)
+        pre = 70  # landed and piling
+    else:
+        # no merge/split: the velocities and positions read after the step are
+        # the ones the upsampling saw
+        desc = workloads.column_collapse(counts=(16, 32, 32), constants="reference", upsample_per=5, adaptive=0)
+        desc["params"].math_mode = 0
+        pre = 30  # collapsing
     s = gg.GranularSystem(**workloads.system_kwargs(desc), device=0)
-    s.step(70)  # landed and piling
+    s.step(pre)
     refs = {fma: _ref_from(kernels[fma], s, desc) for fma in (False, True)}
     for r in refs.values():
         r.neighbor_search()  # the step-start grids the kernel reads
