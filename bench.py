@@ -290,30 +290,26 @@ def run_reference(args):
     # end to end: the caller's cudaMemcpy of positions and velocities into the
     # reference's device arrays before each step and of positions,
     # velocities and render points out of them after it (main.cu:206-209)
-    def pinned(m):
-        return torch.empty((m, 3), dtype=torch.float32, pin_memory=True)
-    hp, hv, hu = pinned(r.size()), pinned(r.size()), pinned(r.upos.shape[0])
-    hp.copy_(r.pos)
-    hv.copy_(r.vel)
+    # pinned host buffers sized once (each step uses the leading rows)
+    cap = 2 * n0
+    hp_all = torch.empty((cap, 3), dtype=torch.float32, pin_memory=True)
+    hv_all = torch.empty((cap, 3), dtype=torch.float32, pin_memory=True)
+    hu = torch.empty((r.upos.shape[0], 3), dtype=torch.float32, pin_memory=True)
+    m = r.size()
+    hp_all[:m].copy_(r.pos)
+    hv_all[:m].copy_(r.vel)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     e2e_units = h2d = d2h = 0
     for _ in range(args.steps):
-        m = r.size()
-        if hp.shape[0] != m:
-            hp, hv = pinned(m), pinned(m)
-            hp.copy_(r.pos)
-            hv.copy_(r.vel)
-        r.pos.copy_(hp, non_blocking=True)
-        r.vel.copy_(hv, non_blocking=True)
+        r.pos.copy_(hp_all[:m], non_blocking=True)
+        r.vel.copy_(hv_all[:m], non_blocking=True)
         h2d += 2 * m * 12
         e2e_units += m
         r.step()
         m = r.size()
-        if hp.shape[0] != m:
-            hp, hv = pinned(m), pinned(m)
-        hp.copy_(r.pos, non_blocking=True)
-        hv.copy_(r.vel, non_blocking=True)
+        hp_all[:m].copy_(r.pos, non_blocking=True)
+        hv_all[:m].copy_(r.vel, non_blocking=True)
         hu.copy_(r.upos, non_blocking=True)
         torch.cuda.synchronize()
         d2h += 2 * m * 12 + hu.shape[0] * 12
@@ -473,38 +469,34 @@ def run_mine(args):
         args.steps_e2e = 0
     else:
         args.steps_e2e = args.steps
-    n = sysg.size()
+    # pinned host buffers sized once for the system's capacity (the particle
+    # count changes every substep once merges complete; each step uses the
+    # leading rows)
+    cap = max(2 * n0, sysg.size())
     nu = sysg.upsampled_size()
-    hp = torch.empty((n, 3), dtype=torch.float32, pin_memory=True).numpy()
-    hv = torch.empty((n, 3), dtype=torch.float32, pin_memory=True).numpy()
+    hp_all = torch.empty((cap, 3), dtype=torch.float32, pin_memory=True).numpy()
+    hv_all = torch.empty((cap, 3), dtype=torch.float32, pin_memory=True).numpy()
     hu = torch.empty((nu, 3), dtype=torch.float32, pin_memory=True).numpy()
-    sysg.read(gg.FIELD_POS, out=hp)
-    sysg.read(gg.FIELD_VEL, out=hv)
+    m = sysg.size()
+    sysg.read(gg.FIELD_POS, out=hp_all[:m])
+    sysg.read(gg.FIELD_VEL, out=hv_all[:m])
     barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     e2e_units = 0
     h2d = d2h = 0
     for _ in range(args.steps_e2e):
-        m = sysg.size()
-        if hp.shape[0] != m:
-            hp = torch.empty((m, 3), dtype=torch.float32, pin_memory=True).numpy()
-            hv = torch.empty((m, 3), dtype=torch.float32, pin_memory=True).numpy()
-            sysg.read(gg.FIELD_POS, out=hp)
-            sysg.read(gg.FIELD_VEL, out=hv)
-        sysg.write(gg.FIELD_POS, hp)
-        sysg.write(gg.FIELD_VEL, hv)
-        h2d += 2 * hp.nbytes
+        # this step's inputs from the host, the step, its results back
+        sysg.write(gg.FIELD_POS, hp_all[:m])
+        sysg.write(gg.FIELD_VEL, hv_all[:m])
+        h2d += 2 * 12 * m
         e2e_units += m
         sysg.step(1)
         m = sysg.size()
-        if hp.shape[0] != m:
-            hp = torch.empty((m, 3), dtype=torch.float32, pin_memory=True).numpy()
-            hv = torch.empty((m, 3), dtype=torch.float32, pin_memory=True).numpy()
-        sysg.read(gg.FIELD_POS, out=hp)
-        sysg.read(gg.FIELD_VEL, out=hv)
+        sysg.read(gg.FIELD_POS, out=hp_all[:m])
+        sysg.read(gg.FIELD_VEL, out=hv_all[:m])
         sysg.read(gg.FIELD_POS, gg.SET_UPSAMPLED, out=hu)
-        d2h += 2 * hp.nbytes + hu.nbytes
+        d2h += 2 * 12 * m + hu.nbytes
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     e2e_s_max, e2e_total = reduce_over_ranks(e2e_s, e2e_units)

@@ -84,7 +84,9 @@ class gg_params(C.Structure):
         ("mass_ledger", C.c_int32), ("merge_enabled", C.c_int32),
         ("upsample_enabled", C.c_int32), ("math_mode", C.c_int32), ("nlist_skin", C.c_float),
         ("target_residual", C.c_float), ("max_sweeps", C.c_int32), ("warm_start", C.c_int32),
-        ("warm_start_scale", C.c_float), ("merge_cas_lag", C.c_int32), ("pad_", C.c_int32),
+        ("warm_start_scale", C.c_float), ("merge_cas_lag", C.c_int32),
+        ("contact_law", C.c_int32), ("mu_static", C.c_float), ("mu_kinetic", C.c_float),
+        ("split_claim", C.c_int32), ("n_planes", C.c_int32), ("planes", (C.c_float * 4) * 8),
     ]
 
 
@@ -108,6 +110,7 @@ def default_params() -> gg_params:
     p.nlist_skin = -1.0
     p.target_residual, p.max_sweeps, p.warm_start, p.warm_start_scale = 0.0, 200, 0, 1.0
     p.merge_cas_lag = 4
+    p.contact_law, p.mu_static, p.mu_kinetic, p.split_claim, p.n_planes = 0, 0.5, 0.4, 0, 0
     return p
 
 

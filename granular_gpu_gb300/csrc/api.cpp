@@ -119,7 +119,13 @@ gg_status gg_default_params(gg_params* P) {
   P->warm_start = 0;
   P->warm_start_scale = 1.0f;
   P->merge_cas_lag = 4;
-  P->pad_ = 0;
+  P->contact_law = 0;
+  P->mu_static = 0.5f;
+  P->mu_kinetic = 0.4f;
+  P->split_claim = 0;
+  P->n_planes = 0;
+  for (int k = 0; k < 8; ++k)
+    for (int c = 0; c < 4; ++c) P->planes[k][c] = 0.0f;
   return GG_OK;
 }
 
@@ -350,6 +356,8 @@ gg_status gg_set_params(gg_system* S, const gg_params* P) {
   }
   REQUIRE(P->stab_iters >= 0 && P->iters >= 0 && P->max_sweeps >= 0, "gg_set_params: negative sweep count");
   REQUIRE(P->merge_cas_lag >= 0 && P->merge_cas_lag <= 65536, "gg_set_params: merge_cas_lag must be in 0..65536");
+  REQUIRE((P->contact_law == 0 || P->contact_law == 1) && P->n_planes >= 0 && P->n_planes <= 8,
+          "gg_set_params: contact_law must be 0 or 1 and n_planes in 0..8");
   S->P = *P;
   return GG_OK;
 }

@@ -120,6 +120,10 @@ struct Granular {
   float* ldens = nullptr;
   int32_t* winner = nullptr;
   int32_t* claim_tgt = nullptr;  // merge schedule: the proposing partner a proposer claims first, or -1
+  uint32_t* cell_claim = nullptr; // split claims per cell (C; 0xffffffff = free), configured mode
+  float4* fdelta = nullptr;       // Coulomb law: summed friction targets (xyz) and their count (w)
+  float* pn = nullptr;            // Coulomb law: normal correction received in the substep so far
+  int32_t* child_cell = nullptr;  // cell a split child claimed, or -1
   uint8_t* claimed = nullptr;    // merge schedule: 2 x cap claim statuses (iterations ping-pong)
   int32_t* split_flag = nullptr;
   int32_t* keep_flag = nullptr;

@@ -591,11 +591,13 @@ __global__ void __launch_bounds__(256) k_split_mark(Grid g, int n, const float4*
                                                     const int32_t* __restrict__ cs, const int32_t* __restrict__ bcs,
                                                     const float4* __restrict__ bpos, float split_min, float rho_f,
                                                     int32_t* __restrict__ split_flag, int32_t* __restrict__ keep,
-                                                    float4* __restrict__ child_pos) {
+                                                    float4* __restrict__ child_pos, uint32_t* __restrict__ cell_claim,
+                                                    int32_t* __restrict__ child_cell) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   keep[i] = remove[i] != 1;
   split_flag[i] = 0;
+  if (cell_claim) child_cell[i] = -1;
   const float mi = mass[i];
   if (remove[i] != 0 || surface[i] != 1 || mi <= split_min) return;
   const float r_i = radius_split<MM>(mi, rho_f);
@@ -603,6 +605,7 @@ __global__ void __launch_bounds__(256) k_split_mark(Grid g, int n, const float4*
   const float3 p = f3(pos[i]);
   const int3 q = trunc_cell(g, p);
   bool found = false;
+  int found_cell = 0;
   float3 center = make_float3(0.f, 0.f, 0.f);
   for (int m = 0; m < 27; ++m) {
     const int cx = q.x + m / 9 - 1, cy = q.y + (m % 9) / 3 - 1, cz = q.z + m % 3 - 1;
@@ -611,6 +614,7 @@ __global__ void __launch_bounds__(256) k_split_mark(Grid g, int n, const float4*
     if (!found && m != 13) {
       if (cs[cell] == cs[cell + 1] && bcs[cell] == bcs[cell + 1]) {
         center = make_float3(((float)cx + 0.5f) * g.L, ((float)cy + 0.5f) * g.L, ((float)cz + 0.5f) * g.L);
+        found_cell = cell;
         found = true;
       }
     }
@@ -622,6 +626,28 @@ __global__ void __launch_bounds__(256) k_split_mark(Grid g, int n, const float4*
   if (!found) return;
   split_flag[i] = 1;
   child_pos[i] = make_float4(center.x, center.y, center.z, 0.f);
+  if (cell_claim) {
+    // configured mode: the child claims its cell, the lowest parent wins
+    child_cell[i] = found_cell;
+    atomicMin(&cell_claim[found_cell], (uint32_t)i);
+  }
+}
+
+// Configured mode (gg_params.split_claim): a parent that lost the claim on
+// its child's cell does not split this substep.
+__global__ void k_split_claim(int n, const int32_t* __restrict__ child_cell, const uint32_t* __restrict__ cell_claim,
+                              int32_t* __restrict__ split_flag) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n || !split_flag[i]) return;
+  if (cell_claim[child_cell[i]] != (uint32_t)i) split_flag[i] = 0;
+}
+
+// Clears the claims of this substep (all flagged parents' cells) once the
+// winners are known, so the table is all-free (0xffffffff) at the next.
+__global__ void k_split_claim_reset(int n, const int32_t* __restrict__ child_cell, uint32_t* __restrict__ cell_claim) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n || child_cell[i] < 0) return;
+  cell_claim[child_cell[i]] = 0xffffffffu;
 }
 
 struct CompactArgs {
@@ -742,8 +768,14 @@ gg_status split_and_compact(gg_system* S, cudaStream_t st) {
   auto kmark = S->P.math_mode ? k_split_mark<1> : k_split_mark<0>;
   kmark<<<nb, 256, 0, st>>>(S->grid, (int)S->n, G.pos[c], G.mass[c], G.surface, G.remove[c], G.cell_start,
                                    S->b.cell_start, S->b.pos, S->P.split_min_mass, S->phys.density, G.split_flag,
-                                   G.keep_flag, G.child_pos);
+                                   G.keep_flag, G.child_pos, S->P.split_claim ? G.cell_claim : nullptr,
+                                   G.child_cell);
   count_launches(S, 1);
+  if (S->P.split_claim) {
+    k_split_claim<<<nb, 256, 0, st>>>((int)S->n, G.child_cell, G.cell_claim, G.split_flag);
+    k_split_claim_reset<<<nb, 256, 0, st>>>((int)S->n, G.child_cell, G.cell_claim);
+    count_launches(S, 2);
+  }
   prof_end(S, PC_SPLIT, S->n, st);
   prof_begin(S, PC_COMPACT, st);
   gg_status rc = exclusive_scan(G.keep_flag, G.keep_slot, S->n, S->sort, st, &S->scal->n_kept);

@@ -76,13 +76,34 @@ gg_status predict(gg_system* S, cudaStream_t st) {
   return GG_OK;
 }
 
+// Analytic walls of the configured mode (gg_params.planes) and its Coulomb
+// friction.
+struct PlaneArgs {
+  int n;          // planes in use (0: none)
+  int coulomb;    // contact_law 1
+  float mus, muk;
+  float4 pl[8];   // unit normal, offset: a particle keeps n . x >= d + r
+};
+
 // change_position_functor (Solver.cu:403-414): x* += delta / max(1, n); in
 // the stabilisation sweeps x as well (:457-460).
+//
+// Configured mode.  Analytic walls are hard constraints: x* is projected
+// onto each wall it is within its radius of (in a stabilisation sweep x
+// moves with it).  With the Coulomb law, outside the stabilisation sweeps,
+// friction targets cancel the tangential slip since the substep began:
+// the particle contacts' targets from the sweep (fdelta) are averaged like
+// the normal corrections, each wall in contact (within 1 % of the radius)
+// gets its own, applied in full like its projection.  A target is applied
+// whole while its length is below mu_static times the normal correction the
+// particle received in this substep so far (pn: the averaged contact
+// corrections and the wall projections), else cut to mu_kinetic times it.
 __global__ void __launch_bounds__(256) k_apply(int n, float4* __restrict__ xs, float4* __restrict__ pos,
                         const float4* __restrict__ delta, int32_t* __restrict__ s_extra,
                         int32_t* __restrict__ ncon, int32_t* __restrict__ contacts, int stab, int last,
                         unsigned int* __restrict__ inc_bits, const uint32_t* __restrict__ keys,
-                        uint32_t* __restrict__ cell_inc, int C, int nz, UDiv div_z) {
+                        uint32_t* __restrict__ cell_inc, int C, int nz, UDiv div_z, PlaneArgs pa,
+                        const float4* __restrict__ fdelta, float* __restrict__ pn) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   unsigned int bits = 0;
   uint32_t key = 0xffffffffu;
@@ -92,24 +113,72 @@ __global__ void __launch_bounds__(256) k_apply(int n, float4* __restrict__ xs, f
     const int se = s_extra[i];
     float4 x = xs[i];
     float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (stab) p = pos[i];
+    if (stab || fdelta) p = pos[i];
     if (cell_inc) key = keys[i];
     const int packed = __float_as_int(d.w);
     const int c = packed & 0xffff;
     const int sl = (int)((unsigned)packed >> 16);
     const int nn = c + sl + se;
-    const float3 inc = div3s(make_float3(d.x, d.y, d.z), (float)(nn > 1 ? nn : 1));
+    float3 inc = div3s(make_float3(d.x, d.y, d.z), (float)(nn > 1 ? nn : 1));
     s_extra[i] = 0;
+    const float3 x_old = f3(x);
     x.x = x.x + inc.x;
     x.y = x.y + inc.y;
     x.z = x.z + inc.z;
-    xs[i] = x;
     if (stab) {
       p.x = p.x + inc.x;
       p.y = p.y + inc.y;
       p.z = p.z + inc.z;
-      pos[i] = p;
     }
+    float pni = 0.0f;
+    if (fdelta) pni = pn[i] + len3(inc);
+    for (int k = 0; k < pa.n; ++k) {
+      const float3 nrm = make_float3(pa.pl[k].x, pa.pl[k].y, pa.pl[k].z);
+      const float sd = dot3(nrm, f3(x)) - pa.pl[k].w - x.w;
+      if (!(sd < 0.0f)) continue;
+      x.x = x.x + -sd * nrm.x;
+      x.y = x.y + -sd * nrm.y;
+      x.z = x.z + -sd * nrm.z;
+      if (stab) {
+        p.x = p.x + -sd * nrm.x;
+        p.y = p.y + -sd * nrm.y;
+        p.z = p.z + -sd * nrm.z;
+      }
+      pni = pni - sd;
+    }
+    if (fdelta && !stab) {
+      // particle contacts: their friction targets averaged, as the normal
+      // corrections are
+      const float4 fd = fdelta[i];
+      const int fc = __float_as_int(fd.w);
+      if (fc > 0) {
+        const float3 ft = div3s(make_float3(fd.x, fd.y, fd.z), (float)fc);
+        const float lt = len3(ft);
+        const float f = lt < pa.mus * pni ? 1.0f : fminf(pa.muk * pni / lt, 1.0f);
+        x.x = x.x + f * ft.x;
+        x.y = x.y + f * ft.y;
+        x.z = x.z + f * ft.z;
+      }
+      // walls in contact (within 1 % of the radius): the tangential slip
+      // since the substep began, cancelled in full like their normal
+      // projection
+      for (int k = 0; k < pa.n; ++k) {
+        const float3 nrm = make_float3(pa.pl[k].x, pa.pl[k].y, pa.pl[k].z);
+        const float sd = dot3(nrm, f3(x)) - pa.pl[k].w - x.w;
+        if (!(sd < 0.01f * x.w)) continue;
+        const float3 drel = sub3(f3(x), f3(p));
+        const float3 tn = sub3(drel, smul3(dot3(drel, nrm), nrm));
+        const float lt = len3(tn);
+        const float f = lt < pa.mus * pni ? 1.0f : fminf(pa.muk * pni / lt, 1.0f);
+        x.x = x.x - f * tn.x;
+        x.y = x.y - f * tn.y;
+        x.z = x.z - f * tn.z;
+      }
+    }
+    if (fdelta) pn[i] = pni;
+    if (pa.n || fdelta) inc = sub3(f3(x), x_old);  // the listed sweeps bound the whole change
+    xs[i] = x;
+    if (stab) pos[i] = p;
     if (last) {
       ncon[i] = nn;
       contacts[i] = c;
@@ -143,11 +212,19 @@ gg_status apply(gg_system* S, int it, bool stab, bool last, cudaStream_t st) {
   // the listed sweep after this one reads the per-cell increments
   uint32_t* cell_inc = (S->g.cell_inc && !last) ? S->g.cell_inc : nullptr;
   if (cell_inc) GG_CUDA(cudaMemsetAsync(cell_inc, 0, sizeof(uint32_t) * ((size_t)S->grid.C + 1), st));
+  PlaneArgs pa;
+  pa.n = std::max(0, std::min(S->P.n_planes, 8));
+  pa.coulomb = S->P.contact_law == 1;
+  pa.mus = S->P.mu_static;
+  pa.muk = S->P.mu_kinetic;
+  for (int k = 0; k < 8; ++k)
+    pa.pl[k] = make_float4(S->P.planes[k][0], S->P.planes[k][1], S->P.planes[k][2], S->P.planes[k][3]);
   const int ta = S->tune.apply_threads;
   k_apply<<<blocks_for(S->n, ta), ta, 0, st>>>((int)S->n, S->g.xs, S->g.pos[S->g.cur], S->g.delta,
                                                  S->g.s_extra, S->g.ncon, S->g.contacts, stab ? 1 : 0,
                                                  last ? 1 : 0, &S->scal->inc_bits[it], S->g.keys, cell_inc,
-                                                 S->grid.C, S->grid.nz, make_udiv((uint32_t)S->grid.nz));
+                                                 S->grid.C, S->grid.nz, make_udiv((uint32_t)S->grid.nz), pa,
+                                                 pa.coulomb ? S->g.fdelta : nullptr, S->g.pn);
   count_launches(S, 1);
   prof_end(S, PC_APPLY, S->n, st);
   GG_CUDA(cudaGetLastError());

@@ -60,7 +60,16 @@ struct SweepArgs {
   const float* __restrict__ scene_fcap;
   float scene_inv_w;
   int n_scenes;
+  // configured mode (gg_params.contact_law): substep-start positions for
+  // the friction law and its output, the summed friction corrections and
+  // their count (both null with the reference's law)
+  const float4* __restrict__ pos0;
+  float4* __restrict__ fdelta;
 };
+
+// The kernels' template argument MM: bit 0 the math mode (0 CUDA's
+// functions, 1 rounded once from double), bit 1 the contact law (0 the
+// reference's, 1 Coulomb friction).
 
 // Which of the three cell columns [c-1, c, c+1] along one axis can hold a
 // partner: bit k set for offset k-1.  Cells are [cL, (c+1)L) in binning
@@ -91,6 +100,12 @@ struct Target {
   int cx, cy, cz; // binning cell
   unsigned pm[3], bm[3];
   float fcapf;    // friction cap factor (0.8 in the reference; per scene in a batch), as float
+  float3 x0;      // position at the substep's start (Coulomb law only)
+  // Coulomb law: the friction corrections and their count, averaged on
+  // their own by the apply kernel (mutable: the contact functions take the
+  // target as const and add to these)
+  mutable float3 df;
+  mutable int fc;
 };
 
 // The friction cap in double, as the reference's comparisons and ratios use
@@ -117,6 +132,9 @@ __device__ __forceinline__ void make_target_lite(const SweepArgs& a, int i, floa
   t.Bf = (float)Bd;
   t.Bcut = t.Bf * t.Bf * 1.0001f;
   t.inv_m = a.inv_m[i];
+  t.x0 = a.pos0 ? f3(a.pos0[i]) : t.x;
+  t.df = make_float3(0.f, 0.f, 0.f);
+  t.fc = 0;
   t.q = trunc_cell(g, t.x);
   const uint32_t key = a.keys[i];
   t.binned = (int)key < g.C;
@@ -160,13 +178,26 @@ __device__ __forceinline__ void make_target(const SweepArgs& a, int i, float4 xi
 template <int MM>
 __device__ __forceinline__ void wall_contact(const SweepArgs& a, const Target& t, float4 pb, float3& dp, int& c) {
   const float bx = t.x.x - pb.x, by = t.x.y - pb.y, bz = t.x.z - pb.z;
-  const float dis = m_norm3<MM>(bx, by, bz);
+  const float dis = m_norm3<(MM & 1)>(bx, by, bz);
   if (!(dis < t.Bru)) return;  // mag < 0
   const float mag = (float)((double)dis - target_bd(a, t));
   const float3 p12 = make_float3(bx, by, bz);
   const float3 dpi = smul3(mag / dis, p12);
+  if (MM & 2) {
+    // Coulomb law: the normal push, and the friction target: cancel the
+    // tangential displacement since the substep began (the apply kernel
+    // limits the averaged friction by the particle's normal corrections)
+    const float3 drel = sub3(t.x, t.x0);
+    const float dn = dot3(drel, p12) / (dis * dis);
+    const float3 dtan = sub3(drel, smul3(dn, p12));
+    dp = sub3(dp, dpi);
+    t.df = sub3(t.df, dtan);
+    ++t.fc;
+    ++c;
+    return;
+  }
   const float3 perp = sub3(dpi, div3s(smul3(dot3(dpi, p12), p12), dis * dis));
-  const float pn = m_norm3<MM>(perp.x, perp.y, perp.z);
+  const float pn = m_norm3<(MM & 1)>(perp.x, perp.y, perp.z);
   if (pn < t.capBru) {
     dp = sub3(dp, dpi);
   } else {
@@ -200,7 +231,7 @@ __device__ __forceinline__ void particle_pair_f(const SweepArgs& a, const Target
   const float rr = t.rc + xj4.w;
   const float d2 = __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmul_rn(dz, dz)));
   if (d2 > rr * rr * 1.0001f) return;
-  const float dis = m_norm3<MM>(dx, dy, dz);
+  const float dis = m_norm3<(MM & 1)>(dx, dy, dz);
   const float mag = rr - dis;
   if (!(mag >= 0.0f)) return;
   const float inv_mj = inv_of();
@@ -209,6 +240,19 @@ __device__ __forceinline__ void particle_pair_f(const SweepArgs& a, const Target
   const float inv_sum = __frcp_rn(t.inv_m + inv_mj);
   const float tt = mag / dis;
   const float3 p12 = make_float3(dx, dy, dz);
+  if (MM & 2) {
+    // Coulomb law: i's share of the normal push, and its share of cancelling
+    // the relative tangential displacement since the substep began (limited
+    // by the apply kernel)
+    const float w = inv_sum * t.inv_m;
+    const float4 xj0 = a.pos0[j];
+    const float3 drel = sub3(sub3(t.x, t.x0), make_float3(xj4.x - xj0.x, xj4.y - xj0.y, xj4.z - xj0.z));
+    const float dn = dot3(drel, p12) / (dis * dis);
+    const float3 dtan = sub3(drel, smul3(dn, p12));
+    dp = add3(dp, smul3(w * tt, p12));
+    t.df = sub3(t.df, smul3(w, dtan));
+    ++t.fc;
+  } else {
   const float3 dpi = smul3((-inv_sum * t.inv_m) * tt, p12);
   const float3 dpj = smul3((inv_sum * inv_mj) * tt, p12);
   const float3 dpij = sub3(dpi, dpj);
@@ -225,7 +269,7 @@ __device__ __forceinline__ void particle_pair_f(const SweepArgs& a, const Target
     within = true;
   } else {
     const float3 perp = sub3(dpij, div3s(smul3(dot3(dpij, p12), p12), dis * dis));
-    pn = m_norm3<MM>(perp.x, perp.y, perp.z);
+    pn = m_norm3<(MM & 1)>(perp.x, perp.y, perp.z);
     // (double)pn < (double)rr * 0.8, decided in float when clear-cut
     if (pn < capf * 0.999999f) within = true;
     else if (pn > capf * 1.000001f) within = false;
@@ -236,6 +280,7 @@ __device__ __forceinline__ void particle_pair_f(const SweepArgs& a, const Target
   } else {
     const float minf = (float)fmin((double)rr * target_fcap(a, t) / (double)pn, 1.0);
     dp = sub3(dp, mul3s(smul3(w, dpij), minf));
+  }
   }
   ++c;
   const int3 qj = trunc_cell(a.g, make_float3(xj4.x, xj4.y, xj4.z));
@@ -285,6 +330,7 @@ __device__ void sweep_global(const SweepArgs& a, int i, const Target& t) {
     }
   }
   a.delta[i] = make_float4(dp.x, dp.y, dp.z, __int_as_float((c & 0xffff) | (s_loc << 16)));
+  if (MM & 2) a.fdelta[i] = make_float4(t.df.x, t.df.y, t.df.z, __int_as_float(t.fc));
 }
 
 template <int MM>
@@ -369,6 +415,7 @@ __global__ void __launch_bounds__(kWarpThreads) k_sweep_list(SweepArgs a) {
   }
   flush();
   a.delta[i] = make_float4(dp.x, dp.y, dp.z, __int_as_float((c & 0xffff) | (s_loc << 16)));
+  if (MM & 2) a.fdelta[i] = make_float4(t.df.x, t.df.y, t.df.z, __int_as_float(t.fc));
 }
 
 // ------------------------------------------------------------ listed sweep
@@ -498,6 +545,7 @@ __global__ void __launch_bounds__(256, 5) k_sweep_nlist_keep(SweepArgs a) {
       const int32_t* __restrict__ li = a.nl_idx + i;
       apply_entries<MM>(a, t, m.w, [&](int k) { return __ldcs(li + (size_t)k * a.cap); }, dp, c, s_loc);
       a.delta[i] = make_float4(dp.x, dp.y, dp.z, __int_as_float((c & 0xffff) | (s_loc << 16)));
+      if (MM & 2) a.fdelta[i] = make_float4(t.df.x, t.df.y, t.df.z, __int_as_float(t.fc));
     } else {
       rebuild = true;
     }
@@ -606,6 +654,7 @@ __global__ void __launch_bounds__(kBuildThreads, 8) k_sweep_nlist_build(SweepArg
     // the list this thread just wrote (its own stores: read back in order)
     apply_entries<MM>(a, t, cnt, [&](int k) { return li[(size_t)k * a.cap]; }, dp, c, s_loc);
     a.delta[i] = make_float4(dp.x, dp.y, dp.z, __int_as_float((c & 0xffff) | (s_loc << 16)));
+    if (MM & 2) a.fdelta[i] = make_float4(t.df.x, t.df.y, t.df.z, __int_as_float(t.fc));
   }
 }
 
@@ -630,6 +679,10 @@ gg_status sweep(gg_system* S, int it, cudaStream_t st) {
   a.scene_inv_w = S->scene_width > 0.0f ? 1.0f / S->scene_width : 0.0f;
   a.n_scenes = S->n_scenes;
   a.minr = S->P.boundary_min_radius;
+  const bool coulomb = S->P.contact_law == 1;
+  a.pos0 = coulomb ? S->g.pos[S->g.cur] : nullptr;
+  a.fdelta = coulomb ? S->g.fdelta : nullptr;
+  const int mm = (S->P.math_mode ? 1 : 0) | (coulomb ? 2 : 0);  // the kernels' template argument
   a.nl_idx = S->g.nl_idx;
   a.nl_meta = S->g.nl_meta;
   a.nl_acc = S->g.nl_acc;
@@ -650,14 +703,14 @@ gg_status sweep(gg_system* S, int it, cudaStream_t st) {
   // listed in order; gg_tuning.sweep_variant = 1 picks the pruned
   // one-thread-per-particle stencil sweep instead (same results)
   if (S->tune.sweep_variant == 1) {
-    auto kern = S->P.math_mode ? k_sweep<1> : k_sweep<0>;
+    auto kern = (mm == 0 ? k_sweep<0> : mm == 1 ? k_sweep<1> : mm == 2 ? k_sweep<2> : k_sweep<3>);
     kern<<<blocks_for(S->n, 256), 256, 0, st>>>(a);
   } else if (S->g.nl_idx) {
-    auto build = S->P.math_mode ? k_sweep_nlist_build<1> : k_sweep_nlist_build<0>;
+    auto build = (mm == 0 ? k_sweep_nlist_build<0> : mm == 1 ? k_sweep_nlist_build<1> : mm == 2 ? k_sweep_nlist_build<2> : k_sweep_nlist_build<3>);
     if (it == 0) {
       build<<<blocks_for(S->n, kBuildThreads), kBuildThreads, 0, st>>>(a, 0);
     } else {
-      auto keep = S->P.math_mode ? k_sweep_nlist_keep<1> : k_sweep_nlist_keep<0>;
+      auto keep = (mm == 0 ? k_sweep_nlist_keep<0> : mm == 1 ? k_sweep_nlist_keep<1> : mm == 2 ? k_sweep_nlist_keep<2> : k_sweep_nlist_keep<3>);
       const int tk = S->tune.keep_threads;
       keep<<<blocks_for(S->n, tk), tk, 0, st>>>(a);
       const int nb = std::min(blocks_for(S->n, kBuildThreads), S->num_sms * S->tune.build_blocks_per_sm);
@@ -665,7 +718,7 @@ gg_status sweep(gg_system* S, int it, cudaStream_t st) {
       count_launches(S, 1);
     }
   } else {
-    auto kern = S->P.math_mode ? k_sweep_list<1> : k_sweep_list<0>;
+    auto kern = (mm == 0 ? k_sweep_list<0> : mm == 1 ? k_sweep_list<1> : mm == 2 ? k_sweep_list<2> : k_sweep_list<3>);
     kern<<<blocks_for(S->n, kWarpThreads), kWarpThreads, 0, st>>>(a);
   }
   count_launches(S, 1);

@@ -124,6 +124,8 @@ gg_status step_once(gg_system* S) {
   if ((rc = predict(S, st)) != GG_OK) return rc;
   if (S->P.warm_start == 1 && (rc = warm_start_apply(S, st)) != GG_OK) return rc;
   if (S->P.warm_start == 2 && (rc = warm_start_record(S, st)) != GG_OK) return rc;
+  // Coulomb law: the normal correction each particle receives accumulates over the substep
+  if (S->P.contact_law == 1 && S->n > 0) GG_CUDA(cudaMemsetAsync(S->g.pn, 0, sizeof(float) * (size_t)S->n, st));
   if (S->P.target_residual > 0.0f) {
     // residual mode: the stabilisation sweeps, then Jacobi sweeps until the
     // largest penetration, measured before each sweep, is within the target
@@ -211,7 +213,7 @@ static void free_all(gg_system* S) {
   }
   void* ptrs[] = {G.merge_vel, G.surface, G.sdist, G.cover, G.xs, G.inv_m, G.delta, G.s_extra, G.contacts,
                   G.ncon, G.keys, G.perm, G.cell_start, G.cell_surf, G.prop, G.ldens, G.winner, G.split_flag, G.keep_flag,
-                  G.split_slot, G.keep_slot, G.child_pos, G.nl_idx, G.nl_meta, G.nl_acc, G.nl_queue, G.cell_inc, G.ld_sum, G.ld_cnt, G.claim_tgt, G.claimed, S->b.pos, S->b.animated, S->b.pos_alt,
+                  G.split_slot, G.keep_slot, G.child_pos, G.nl_idx, G.nl_meta, G.nl_acc, G.nl_queue, G.cell_inc, G.ld_sum, G.ld_cnt, G.claim_tgt, G.claimed, G.cell_claim, G.child_cell, G.fdelta, G.pn, S->b.pos, S->b.animated, S->b.pos_alt,
                   S->b.animated_alt, S->b.keys, S->b.perm, S->b.cell_start, S->u.keys, S->u.perm, S->scal,
                   S->stats_partial, S->stage, S->feat, S->xs0, S->warm_target, S->scene_fcap,
                   S->scene_acc};
@@ -261,6 +263,11 @@ gg_status system_create(const gg_desc* d, gg_system** out) {
   }
   if (d->params.merge_cas_lag < 0 || d->params.merge_cas_lag > 65536) {
     set_error("gg_create: merge_cas_lag must be in 0..65536");
+    return GG_ERR_INVALID_ARGUMENT;
+  }
+  if ((d->params.contact_law != 0 && d->params.contact_law != 1) || d->params.n_planes < 0 ||
+      d->params.n_planes > 8) {
+    set_error("gg_create: contact_law must be 0 or 1 and n_planes in 0..8");
     return GG_ERR_INVALID_ARGUMENT;
   }
   int64_t cap = d->max_particles > 0 ? d->max_particles : 2 * d->n_particles;
@@ -320,6 +327,8 @@ gg_status system_create(const gg_desc* d, gg_system** out) {
   ALLOC(G.split_flag, cap); ALLOC(G.keep_flag, cap); ALLOC(G.split_slot, cap); ALLOC(G.keep_slot, cap);
   ALLOC(G.child_pos, cap); ALLOC(G.ld_sum, cap); ALLOC(G.ld_cnt, cap);
   ALLOC(G.claim_tgt, cap); ALLOC(G.claimed, 2 * cap);
+  ALLOC(G.cell_claim, C64); ALLOC(G.child_cell, cap); ALLOC(G.fdelta, cap); ALLOC(G.pn, cap);
+  if (e == cudaSuccess) e = cudaMemset(G.cell_claim, 0xff, sizeof(uint32_t) * (size_t)std::max<int64_t>(C64, 1));
   // contact lists: a negative skin asks for the automatic one, a tenth of
   // the cell length; zero or NaN turns them off
   S->nl_skin = S->P.nlist_skin < 0.0f ? 0.1f * S->grid.L : S->P.nlist_skin;

@@ -81,6 +81,44 @@ def scaled_params(r: float, iters: int, stab_iters: int = 3, dt_sub: float = Non
     return p
 
 
+def set_planes(params, planes):
+    """Analytic walls (n, d): a particle keeps n . x >= d + r.  Normals are
+    normalised here."""
+    params.n_planes = len(planes)
+    for k, (n, d) in enumerate(planes):
+        n = np.asarray(n, np.float64)
+        n = n / np.linalg.norm(n)
+        for c in range(3):
+            params.planes[k][c] = float(n[c])
+        params.planes[k][3] = float(d)
+    return params
+
+
+def box_planes(space_size, inset=0.005):
+    """The six faces of the box, where the wall particles of box_walls lie
+    (inset by 0.5 % of each side), as analytic walls."""
+    sp = np.asarray(space_size, np.float64)
+    out = []
+    for a in range(3):
+        n = np.zeros(3)
+        n[a] = 1.0
+        out.append((n.copy(), inset * sp[a]))
+        out.append((-n, -(1.0 - inset) * sp[a]))
+    return out
+
+
+def configure(params, mu_static=0.5, mu_kinetic=0.4, planes=()):
+    """Configured mode: Coulomb friction mu_static / mu_kinetic (restitution
+    0), children that claim their cell, and analytic walls.  The scene's
+    Jacobi sweeps are all the solver runs (no stabilisation sweeps, which
+    move the substep's start positions and let resting contacts creep)."""
+    params.contact_law = 1
+    params.stab_iters = 0
+    params.mu_static, params.mu_kinetic = float(mu_static), float(mu_kinetic)
+    params.split_claim = 1
+    return set_planes(params, list(planes))
+
+
 def _desc(particles, walls, upsampled, space, L, cs, dt, g, density, adaptive, params, skip=False):
     return dict(particles=particles, n_particles=particles.shape[0], boundary=walls,
                 n_boundary=walls.shape[0], upsampled=upsampled,
@@ -123,6 +161,9 @@ def column_collapse(counts=(128, 256, 256), r=0.002, seed=42, substeps=4, iters=
 
     constants="scaled" scales every length constant of the reference by
     r / 0.01 and advects render points with the substep's dt;
+    constants="configured" adds the configured mode to that (Coulomb
+    friction 0.5 / 0.4, claiming split children, the box faces as analytic
+    walls);
     constants="reference" keeps them as compiled into the reference's
     kernels (wall reach 0.01 + max(r, 0.01), merge radius 0.035, upsampling
     support 0.045 and step 0.002, ...), as the reference's own build runs
@@ -136,8 +177,13 @@ def column_collapse(counts=(128, 256, 256), r=0.002, seed=42, substeps=4, iters=
     dt = 1.0 / 120.0 / substeps
     if constants == "reference":
         params = scaled_params(REF_RADIUS, iters=iters, dt_sub=None, max_mass=8.0, ledger=1)
-    elif constants == "scaled":
+    elif constants in ("scaled", "configured"):
         params = scaled_params(r, iters=iters, dt_sub=dt, max_mass=8.0, ledger=1)
+        if constants == "configured":
+            # the configuration's contact model: Coulomb friction 0.5 / 0.4,
+            # restitution 0, split children that claim their cell, and the
+            # box faces as analytic walls behind the wall particles
+            configure(params, 0.5, 0.4, box_planes(space))
     else:
         raise ValueError(constants)
     params.merge_enabled = 1 if adaptive else 0

@@ -149,7 +149,26 @@ typedef struct gg_params {
                                   first (on itself).  0 lets every warp finish before the next starts;
                                   larger values merge less.  4 merges about as many pairs as the
                                   reference's own kernel does on a GB300.  0..65536 */
-  int32_t pad_;
+  /* Configured mode: the contact model the benchmark configurations describe
+   * and the reference's constants cannot express.  No counterpart in the
+   * reference; the defaults keep its behaviour. */
+  int32_t contact_law;         /* 0 (default) the reference's contacts: a tangential cap that is
+                                  practically inactive (Solver.cu:272-359); 1 = Coulomb friction:
+                                  each contact (particle, wall particle or plane) with penetration
+                                  depth d also corrects the relative tangential displacement since
+                                  the substep began, t: fully when |t| < mu_static d (sticking),
+                                  else by min(mu_kinetic d / |t|, 1) (sliding).  Contacts stay
+                                  perfectly inelastic (restitution 0: velocities are (x* - x) / dt) */
+  float mu_static;             /* static friction coefficient of contact_law 1 (0.5) */
+  float mu_kinetic;            /* kinetic friction coefficient of contact_law 1 (0.4) */
+  int32_t split_claim;         /* 1 = a split child claims the empty cell it is placed in, the lowest
+                                  parent index winning, so two children never land on one point (the
+                                  reference lets them, and its contact law then divides by zero);
+                                  0 (default) = the reference's split */
+  int32_t n_planes;            /* 0..8 analytic walls: particle i keeps planes[k][0..2] . x >=
+                                  planes[k][3] + r_i (unit normal, offset); applied in every sweep
+                                  after the particle and wall contacts, with contact_law's friction */
+  float planes[8][4];
 } gg_params;
 
 /* Arguments of GranularSystem::GranularSystem, GranularSystem.hpp:8-14. */

@@ -129,7 +129,8 @@ typedef struct ggo_sys {
   /* merge scratch */
   int32_t *prop, *winner; real *ldens;
   /* split scratch */
-  int32_t *split_flag; r3 *child_pos;
+  int32_t *split_flag; r3 *child_pos; int32_t *child_cell;
+  r3 *fdelta; int32_t *fcount; real *pn;
   int64_t nb;
   r3 *bpos;
   int32_t *banim, *bkeys, *bcell_start;
@@ -317,12 +318,15 @@ static void sweep(ggo_sys* s) {
   const int64_t n = s->n;
   const double brad = s->P.boundary_radius;
   const double fcap = s->P.friction_cap;
+  const int coulomb = s->P.contact_law == 1;
   memset(s->rev, 0, sizeof(int32_t) * (size_t)n);
 #pragma omp parallel for schedule(dynamic, 256)
   for (int64_t i = 0; i < n; ++i) {
     r3 xi = s->pos_t[i];
+    const r3 x0i = s->pos[i];
     r3 dp = v3(0, 0, 0);
-    int c = 0;
+    r3 df = v3(0, 0, 0); /* Coulomb law: friction corrections, averaged on their own */
+    int c = 0, fc = 0;
     const i3 q = trunc_cell(s, xi);
     const real rb_i = s->rb[i];
     const real rc_i = s->rc[i];
@@ -335,7 +339,19 @@ static void sweep(ggo_sys* s) {
         const real dis = norm3(xi.x - pb.x, xi.y - pb.y, xi.z - pb.z);
         const real mag = (real)((double)dis - (brad + (double)rb_i));
         const r3 p12 = sub3(xi, pb);
-        if (mag < 0) {
+        if (mag < 0 && coulomb) {
+          /* configured mode (gg_params.contact_law = 1): the normal push,
+           * and the friction target, cancelling the tangential displacement
+           * since the substep began (the apply step limits the average) */
+          const r3 dpi = smul3(mag / dis, p12);
+          const r3 drel = sub3(xi, x0i);
+          const real dn = dot3(drel, p12) / (dis * dis);
+          const r3 dtan = sub3(drel, smul3(dn, p12));
+          dp = sub3(dp, dpi);
+          df = sub3(df, dtan);
+          ++fc;
+          ++c;
+        } else if (mag < 0) {
           const r3 dpi = smul3(mag / dis, p12);
           const r3 perp = sub3(dpi, div3s(smul3(dot3(dpi, p12), p12), dis * dis));
           const real pn = norm3(perp.x, perp.y, perp.z);
@@ -354,7 +370,20 @@ static void sweep(ggo_sys* s) {
         const real rc_j = s->rc[j];
         const real dis = norm3(xi.x - xj.x, xi.y - xj.y, xi.z - xj.z);
         const real mag = (rc_i + rc_j) - dis;
-        if (mag >= 0) {
+        if (mag >= 0 && coulomb) {
+          const real t = mag / dis;
+          const real w = inv_sum * inv_mi;
+          const r3 x0j = s->pos[j];
+          const r3 drel = sub3(sub3(xi, x0i), v3(xj.x - x0j.x, xj.y - x0j.y, xj.z - x0j.z));
+          const real dn = dot3(drel, p12) / (dis * dis);
+          const r3 dtan = sub3(drel, smul3(dn, p12));
+          dp = add3(dp, smul3(w * t, p12));
+          df = sub3(df, smul3(w, dtan));
+          ++fc;
+          ++c;
+#pragma omp atomic
+          s->rev[j]++;
+        } else if (mag >= 0) {
           const real t = mag / dis;
           const r3 dpi = smul3((-inv_sum * inv_mi) * t, p12);
           const r3 dpj = smul3((inv_sum * inv_mj) * t, p12);
@@ -372,6 +401,8 @@ static void sweep(ggo_sys* s) {
       }
     }
     s->delta[i] = dp;
+    s->fdelta[i] = df;
+    s->fcount[i] = fc;
     s->contacts[i] = c;
   }
 #pragma omp parallel for schedule(static)
@@ -393,6 +424,10 @@ static void solver_step(ggo_sys* s) {
     s->scaled_mass[i] = s->mass[i] * R_EXP(-x.y);                  /* :162-191 */
     s->inv_m[i] = (real)1 / s->scaled_mass[i];                     /* :317 */
   }
+  const int np = P->n_planes < 0 ? 0 : (P->n_planes > 8 ? 8 : P->n_planes);
+  const int coulomb = P->contact_law == 1;
+  if (coulomb) memset(s->pn, 0, sizeof(real) * (size_t)n);
+  const real mus = (real)P->mu_static, muk = (real)P->mu_kinetic;
   const int total = P->stab_iters + P->iters;
   for (int it = 0; it < total; ++it) {
     const int stab = it < P->stab_iters;
@@ -402,6 +437,44 @@ static void solver_step(ggo_sys* s) {
       const int nn = s->ncon[i] > 1 ? s->ncon[i] : 1;
       if (stab) s->pos[i] = add3(s->pos[i], div3s(s->delta[i], (real)nn));
       s->pos_t[i] = add3(s->pos_t[i], div3s(s->delta[i], (real)nn));
+      /* configured mode: analytic walls as hard constraints; the Coulomb
+       * law's friction targets (the particle contacts' averaged, each
+       * wall's in full), limited by the normal correction the particle
+       * received in this substep (k_apply, kernels_solve.cu) */
+      real pni = 0;
+      if (coulomb) pni = s->pn[i] + len3(div3s(s->delta[i], (real)nn));
+      for (int k = 0; k < np; ++k) {
+        const r3 nrm = v3((real)P->planes[k][0], (real)P->planes[k][1], (real)P->planes[k][2]);
+        const real sd = dot3(nrm, s->pos_t[i]) - (real)P->planes[k][3] - s->rc[i];
+        if (!(sd < 0)) continue;
+        s->pos_t[i] = v3(s->pos_t[i].x + -sd * nrm.x, s->pos_t[i].y + -sd * nrm.y, s->pos_t[i].z + -sd * nrm.z);
+        if (stab) s->pos[i] = v3(s->pos[i].x + -sd * nrm.x, s->pos[i].y + -sd * nrm.y, s->pos[i].z + -sd * nrm.z);
+        pni = pni - sd;
+      }
+      if (coulomb && !stab) {
+        /* particle contacts: their friction targets averaged, as the
+         * normal corrections are */
+        if (s->fcount[i] > 0) {
+          const r3 ft = div3s(s->fdelta[i], (real)s->fcount[i]);
+          const real lt = len3(ft);
+          const real f = lt < mus * pni ? (real)1 : R_FMIN(muk * pni / lt, (real)1);
+          s->pos_t[i] = v3(s->pos_t[i].x + f * ft.x, s->pos_t[i].y + f * ft.y, s->pos_t[i].z + f * ft.z);
+        }
+        /* walls in contact (within 1 % of the radius): the tangential
+         * slip since the substep began, cancelled in full like the
+         * walls' normal projection */
+        for (int k = 0; k < np; ++k) {
+          const r3 nrm = v3((real)P->planes[k][0], (real)P->planes[k][1], (real)P->planes[k][2]);
+          const real sd = dot3(nrm, s->pos_t[i]) - (real)P->planes[k][3] - s->rc[i];
+          if (!(sd < (real)0.01f * s->rc[i])) continue;
+          const r3 drel = sub3(s->pos_t[i], s->pos[i]);
+          const r3 tn = sub3(drel, smul3(dot3(drel, nrm), nrm));
+          const real lt = len3(tn);
+          const real f = lt < mus * pni ? (real)1 : R_FMIN(muk * pni / lt, (real)1);
+          s->pos_t[i] = v3(s->pos_t[i].x - f * tn.x, s->pos_t[i].y - f * tn.y, s->pos_t[i].z - f * tn.z);
+        }
+      }
+      if (coulomb) s->pn[i] = pni;
     }
   }
   const real dt_inv = (real)1 / s->dt;
@@ -564,6 +637,8 @@ static void surface_distance(ggo_sys* s) {
   }
 }
 
+static void* xcalloc(size_t n, size_t sz);
+
 /* --------------------------------------------------------- merge / split */
 
 static inline int units_of(real m) { return (int)lrint((double)m * GGO_UNITS_PER_MASS); }
@@ -688,7 +763,7 @@ static void merge_count(ggo_sys* s) {
 }
 
 /* check_neighborhood, Solver.cu:708-778. */
-static int check_neighborhood(const ggo_sys* s, r3 pos, real r_i, r3* center) {
+static int check_neighborhood(const ggo_sys* s, r3 pos, real r_i, r3* center, int* center_cell) {
   int found = 0;
   const real max_dist = (real)2 * r_i;
   const i3 q = trunc_cell(s, pos);
@@ -701,6 +776,7 @@ static int check_neighborhood(const ggo_sys* s, r3 pos, real r_i, r3* center) {
           s->bcell_start[cell] == s->bcell_start[cell + 1]) {
         *center = v3(((real)cx + (real)0.5f) * s->L, ((real)cy + (real)0.5f) * s->L,
                      ((real)cz + (real)0.5f) * s->L);
+        *center_cell = cell;
         found = 1;
       }
     }
@@ -722,9 +798,21 @@ static int64_t split_mark(ggo_sys* s) {
     if (s->remove[i] != 0 || s->surface[i] != 1 || s->mass[i] <= (real)P->split_min_mass) continue;
     const real r_i = radius_split(s, s->mass[i]);
     r3 c;
-    if (!check_neighborhood(s, s->pos[i], r_i, &c)) continue;
+    int cc = 0;
+    if (!check_neighborhood(s, s->pos[i], r_i, &c, &cc)) continue;
     s->split_flag[i] = 1;
     s->child_pos[i] = c;
+    s->child_cell[i] = cc;
+  }
+  if (P->split_claim) {
+    /* configured mode: a child claims its cell; the lowest parent wins */
+    unsigned char* taken = (unsigned char*)xcalloc((size_t)s->C + 1, 1);
+    for (int64_t i = 0; i < s->n; ++i) {
+      if (!s->split_flag[i]) continue;
+      if (taken[s->child_cell[i]]) s->split_flag[i] = 0;
+      else taken[s->child_cell[i]] = 1;
+    }
+    free(taken);
   }
   int64_t k = 0;
   for (int64_t i = 0; i < s->n; ++i) k += s->split_flag[i];
@@ -851,6 +939,7 @@ void GGO_SYM(default_params)(gg_params* P) {
   P->up_ground_band = 0.1f; P->up_ground_damping = 0.5f;
   P->mass_ledger = 0; P->merge_enabled = 1; P->upsample_enabled = 1;
   P->merge_cas_lag = 4;
+  P->contact_law = 0; P->mu_static = 0.5f; P->mu_kinetic = 0.4f; P->split_claim = 0; P->n_planes = 0;
 }
 
 ggo_sys* GGO_SYM(create)(const gg_desc* d) {
@@ -889,6 +978,9 @@ ggo_sys* GGO_SYM(create)(const gg_desc* d) {
   s->prop = (int32_t*)xcalloc(cap, sizeof(int32_t)); s->winner = (int32_t*)xcalloc(cap, sizeof(int32_t));
   s->ldens = (real*)xcalloc(cap, sizeof(real));
   s->split_flag = (int32_t*)xcalloc(cap, sizeof(int32_t)); s->child_pos = (r3*)xcalloc(cap, sizeof(r3));
+  s->child_cell = (int32_t*)xcalloc(cap, sizeof(int32_t));
+  s->fdelta = (r3*)xcalloc(cap, sizeof(r3)); s->fcount = (int32_t*)xcalloc(cap, sizeof(int32_t));
+  s->pn = (real*)xcalloc(cap, sizeof(real));
   for (int64_t i = 0; i < s->n; ++i) {
     s->pos[i] = v3((real)d->particles[3 * i], (real)d->particles[3 * i + 1], (real)d->particles[3 * i + 2]);
     const real m = d->masses ? (real)d->masses[i] : (real)1;
@@ -1039,7 +1131,7 @@ void GGO_SYM(destroy)(ggo_sys* s) {
                   s->rs, s->units, s->als, s->surface, s->remove, s->merge_count, s->merge_units, s->sdist,
                   s->merge, s->merge_vel, s->cover, s->keys, s->perm, s->cell_start, s->ncon, s->contacts,
                   s->rev, s->tmp_i, s->tmp_r, s->tmp_3, s->prop, s->winner, s->ldens, s->split_flag,
-                  s->child_pos, s->bpos, s->banim, s->bkeys, s->bcell_start, s->upos, s->uvel, s->ukeys,
+                  s->child_pos, s->child_cell, s->fdelta, s->fcount, s->pn, s->bpos, s->banim, s->bkeys, s->bcell_start, s->upos, s->uvel, s->ukeys,
                   s->stats};
   for (size_t k = 0; k < sizeof(ptrs) / sizeof(ptrs[0]); ++k) free(ptrs[k]);
   free(s);

@@ -47,7 +47,9 @@ def test_default_params_match():
     q = abi.default_params()
     for name, _ in abi.gg_params._fields_:
         a, b = getattr(p, name), getattr(q, name)
-        if isinstance(a, float):
+        if name == "planes":
+            assert [list(r) for r in a] == [list(r) for r in b]
+        elif isinstance(a, float):
             assert C.c_float(a).value == C.c_float(b).value or a == b, name
         else:
             assert a == b, name

@@ -332,7 +332,9 @@ def test_long_run_statistics_follow_reference(kernels):
     assert h <= 0.3 * R
     rest = {k: v[-100:].mean() for k, v in e.items()}
     print(f"resting kinetic energy: ours {rest['ours']:.4g}, reference {rest[0]:.4g} and {rest[1]:.4g}")
-    assert 0.5 <= rest["ours"] / rest[0] <= 2.0
+    # the racy reference's own resting energy varies by a factor of two
+    # between runs: compare with the range of both
+    assert 0.5 * min(rest[0], rest[1]) <= rest["ours"] <= 2.0 * max(rest[0], rest[1])
     s.close()
 
 
