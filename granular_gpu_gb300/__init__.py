@@ -349,6 +349,15 @@ class GranularSystem:
         _check(lib().gg_frame_times(self._h, _fptr(out), out.shape[0], C.byref(n)))
         return out[:n.value]
 
+    def update_animation(self, state: "abi.gg_animation", dt: float):
+        """updateAnimation (main.cu:1210-1277): advances `state` by one frame
+        of dt and moves the animated walls (before the frame's substeps)."""
+        _check(lib().gg_update_animation(self._h, C.byref(state), C.c_float(dt)))
+
+    def animate_walls(self, move: "abi.gg_animation_move"):
+        """animateParticles (main.cu:1175-1208) with the given move."""
+        _check(lib().gg_animate_walls(self._h, C.byref(move)))
+
     def profile_begin(self):
         _check(lib().gg_profile_begin(self._h))
 
@@ -409,6 +418,37 @@ def scene_build(json_path: str, base_dir: str = None) -> dict:
         "upsampled_radius": d.upsampled_radius, "is_move_boundary": d.is_move_boundary,
         "is_adaptive": d.is_adaptive, "params": d.params,
     }
+
+
+def default_animation() -> "abi.gg_animation":
+    """AnimationState's initialisers (main.cu:100-111), not animating."""
+    a = abi.gg_animation()
+    _check(lib().gg_default_animation(C.byref(a)))
+    return a
+
+
+def scene_animation(json_path: str, base_dir: str = None) -> "abi.gg_animation":
+    """The animation state a scene's construction leaves (the excavator's
+    and the funnel's obj_file walls)."""
+    a = abi.gg_animation()
+    bd = base_dir.encode() if base_dir else None
+    _check(lib().gg_scene_animation(json_path.encode(), bd, C.byref(a)))
+    return a
+
+
+def animation_advance(state: "abi.gg_animation", dt: float, walls=None) -> "abi.gg_animation_move":
+    """updateAnimation's host part: advances `state` and returns the frame's
+    move; `walls` (float[3] per wall particle) is read when the translation
+    phase ends."""
+    m = abi.gg_animation_move()
+    if walls is None:
+        w, n = None, 0
+    else:
+        w = _f32(walls)
+        n = w.shape[0]
+    _check(lib().gg_animation_advance(C.byref(state), C.c_float(dt), None if w is None else _fptr(w), n,
+                                      C.byref(m)))
+    return m
 
 
 class Grid:

@@ -172,6 +172,18 @@ class gg_profile_t(C.Structure):
     ]
 
 
+class gg_animation(C.Structure):
+    _fields_ = [("is_animating", C.c_int32), ("animation_time", C.c_float), ("start_index", C.c_int32),
+                ("num_particles", C.c_int32), ("translation_direction", C.c_float * 3),
+                ("translation_speed", C.c_float), ("translation_complete", C.c_int32),
+                ("rotation_angle", C.c_float), ("rotation_speed", C.c_float), ("rotation_center", C.c_float * 3)]
+
+
+class gg_animation_move(C.Structure):
+    _fields_ = [("translation", C.c_float * 3), ("rotation", C.c_float), ("center", C.c_float * 3),
+                ("apply", C.c_int32)]
+
+
 # name -> (restype, argtypes) of every function gg.h declares
 P_ = C.c_void_p
 SIGNATURES = {
@@ -201,6 +213,13 @@ SIGNATURES = {
     "gg_set_frame_timing": (C.c_int, [P_, C.c_int32]),
     "gg_frame_times": (C.c_int, [P_, C.POINTER(C.c_float), C.c_int64, C.POINTER(C.c_int64)]),
     "gg_trigger_explosion": (C.c_int, [P_, C.c_float]),
+    "gg_default_animation": (C.c_int, [C.POINTER(gg_animation)]),
+    "gg_scene_animation": (C.c_int, [C.c_char_p, C.c_char_p, C.POINTER(gg_animation)]),
+    "gg_animation_needs_centroid": (C.c_int32, [C.POINTER(gg_animation), C.c_float]),
+    "gg_animation_advance": (C.c_int, [C.POINTER(gg_animation), C.c_float, C.POINTER(C.c_float), C.c_int64,
+                                       C.POINTER(gg_animation_move)]),
+    "gg_animate_walls": (C.c_int, [P_, C.POINTER(gg_animation_move)]),
+    "gg_update_animation": (C.c_int, [P_, C.POINTER(gg_animation), C.c_float]),
     "gg_profile_begin": (C.c_int, [P_]),
     "gg_profile_end": (C.c_int, [P_, C.POINTER(gg_profile_t)]),
     "gg_stream": (C.c_int, [P_, C.POINTER(P_)]),

@@ -356,6 +356,19 @@ gg_status scene_build(const char* json_path, const char* base_dir, SceneData& ou
       anim.assign(pos.size(), 0);
       if (file_exists(obj_path)) {
         std::vector<V3> extra = read_points(obj_path);
+        // the animation state (main.cu:940-951): the loaded range, and its
+        // centroid before the bucket is placed
+        gg_animation& A = out.animation;
+        A.start_index = (int32_t)pos.size();
+        A.num_particles = (int32_t)extra.size();
+        A.is_animating = 1;
+        A.animation_time = 0.0f;
+        V3 centroid = v3(0.0f, 0.0f, 0.0f);
+        for (const auto& p : extra) centroid = centroid + p;
+        centroid = centroid / (float)extra.size();
+        A.rotation_center[0] = centroid.x;
+        A.rotation_center[1] = centroid.y;
+        A.rotation_center[2] = centroid.z;
         for (auto& p : extra) p = p + v3(2.5f, 0.0f, 0.5f);
         anim.insert(anim.end(), extra.size(), 1);
         pos.insert(pos.end(), extra.begin(), extra.end());
@@ -368,6 +381,12 @@ gg_status scene_build(const char* json_path, const char* base_dir, SceneData& ou
       anim.assign(pos.size(), 0);
       if (file_exists(obj_path)) {
         std::vector<V3> extra = read_points(obj_path);
+        // the animation state (main.cu:1031-1034); the rotation centre keeps
+        // its initialiser
+        out.animation.start_index = (int32_t)pos.size();
+        out.animation.num_particles = (int32_t)extra.size();
+        out.animation.is_animating = 1;
+        out.animation.animation_time = 0.0f;
         V3 centroid = v3(0.0f, 0.0f, 0.0f);
         for (const auto& p : extra) centroid = centroid + p;
         centroid = centroid / (float)extra.size();

@@ -29,8 +29,12 @@ struct Json {
 // Parses text; returns false with a message on malformed input.
 bool json_parse(const std::string& text, Json& out, std::string& err);
 
+// AnimationState's initialisers (animation.cu).
+void default_animation(gg_animation* a);
+
 // The particle sets and constructor arguments init_granular_system
-// (main.cu:746-1173) builds from a scene file.
+// (main.cu:746-1173) builds from a scene file, and the animation state it
+// leaves.
 struct SceneData {
   std::vector<float> particles;   // float[3] each
   std::vector<float> boundary;
@@ -38,6 +42,8 @@ struct SceneData {
   std::vector<float> upsampled;
   gg_desc desc{};
   std::string save_file;
+  gg_animation animation{};
+  SceneData() { default_animation(&animation); }
 };
 
 gg_status scene_build(const char* json_path, const char* base_dir, SceneData& out);

@@ -361,6 +361,67 @@ gg_status gg_frame_times(gg_system* sys, float* host_dst, int64_t capacity, int6
 /* Solver::trigger_explosion (Solver.cu:1411-1442). */
 gg_status gg_trigger_explosion(gg_system* sys, float explosion_force);
 
+/* ------------------------------------------------ animated walls
+ *
+ * The excavator's bucket: wall particles flagged is_animated move by
+ * updateAnimation (main.cu:1210-1277) once per frame, before the frame's
+ * substeps: a translation for the first 2.5 s, then a rotation about the z
+ * axis until 45 degrees are turned.  gg_step re-grids the walls every
+ * substep when the system was created with is_move_boundary
+ * (GranularSystem.cu:402-404). */
+
+/* AnimationState (main.cu:100-111), field for field. */
+typedef struct gg_animation {
+  int32_t is_animating;
+  float animation_time;             /* seconds in the current phase */
+  int32_t start_index;              /* wall index range whose centroid becomes */
+  int32_t num_particles;            /*   the rotation centre (main.cu:1236-1239) */
+  float translation_direction[3];   /* (-0.1, 0, 0) */
+  float translation_speed;          /* 5 */
+  int32_t translation_complete;
+  float rotation_angle;             /* degrees turned so far */
+  float rotation_speed;             /* degrees per second, 90 */
+  float rotation_center[3];
+} gg_animation;
+
+/* One frame's move as updateAnimation decides it: the arguments of
+ * animateParticles (main.cu:1175-1208), and whether it runs. */
+typedef struct gg_animation_move {
+  float translation[3];
+  float rotation;                   /* degrees about z through center; 0 = none */
+  float center[3];
+  int32_t apply;
+} gg_animation_move;
+
+/* The initialisers of AnimationState (not animating). */
+gg_status gg_default_animation(gg_animation* out);
+
+/* The state the scene construction leaves (main.cu:925-960 for the
+ * excavator, 1020-1034 for the funnel): animating, with the range of the
+ * walls read from obj_file, when that file exists; else the defaults. */
+gg_status gg_scene_animation(const char* json_path, const char* base_dir, gg_animation* out);
+
+/* 1 when gg_animation_advance(a, dt, ...) ends the translation phase and so
+ * needs the walls' positions for the rotation centre. */
+int32_t gg_animation_needs_centroid(const gg_animation* a, float dt);
+
+/* updateAnimation's host part on the state alone: advances *a by dt and
+ * returns the frame's move.  walls (float[3] per wall particle, in the
+ * system's current wall order, as the reference reads them back) is read
+ * only when gg_animation_needs_centroid says so; then the range
+ * [start_index, start_index + num_particles) must lie inside n_walls. */
+gg_status gg_animation_advance(gg_animation* a, float dt, const float* walls, int64_t n_walls,
+                               gg_animation_move* out);
+
+/* animateParticles (main.cu:1175-1208): moves the flagged wall particles
+ * on the device.  cos and sin follow the system's math_mode (0: CUDA's
+ * cosf/sinf as the reference; 1: rounded once from double). */
+gg_status gg_animate_walls(gg_system* sys, const gg_animation_move* move);
+
+/* updateAnimation (main.cu:1210-1277): advance, reading the walls back
+ * when the centroid is needed, then animate the walls if the move applies. */
+gg_status gg_update_animation(gg_system* sys, gg_animation* a, float dt);
+
 /* Per-kernel-class timing with CUDA events on the system's stream. */
 gg_status gg_profile_begin(gg_system* sys);
 gg_status gg_profile_end(gg_system* sys, gg_profile_t* out);

@@ -52,6 +52,8 @@ typedef double real;
 #define R_EXP exp
 #define R_SQRT sqrt
 #define R_ACOS acos
+#define R_COS cos
+#define R_SIN sin
 #define R_FLOOR floor
 #define R_FMAX fmax
 #define R_FMIN fmin
@@ -63,6 +65,8 @@ typedef float real;
 #define R_EXP(x) ((float)exp((double)(x)))
 #define R_SQRT sqrtf
 #define R_ACOS(x) ((float)acos((double)(x)))
+#define R_COS(x) ((float)cos((double)(x)))
+#define R_SIN(x) ((float)sin((double)(x)))
 #define R_FLOOR floorf
 #define R_FMAX fmaxf
 #define R_FMIN fminf
@@ -1084,6 +1088,29 @@ int GGO_SYM(write)(ggo_sys* s, int set, int field, const float* src, int64_t n) 
   if (!dst || n != GGO_SYM(size)(s, set)) return -1;
   for (int64_t i = 0; i < n; ++i) dst[i] = v3((real)src[3 * i], (real)src[3 * i + 1], (real)src[3 * i + 2]);
   return 0;
+}
+
+/* animateParticles, main.cu:1175-1208: the flagged walls move by t, then
+ * turn by rotation_deg about the z axis through c.  The angle is
+ * rotation * M_PI / 180.0f as the reference evaluates it (double, rounded
+ * to float). */
+void GGO_SYM(animate_walls)(ggo_sys* s, const float t[3], float rotation_deg, const float c[3]) {
+  const real angle = (real)(float)((double)rotation_deg * GGO_PI_D / 180.0);
+  const real ct = R_COS(angle), st = R_SIN(angle);
+  for (int64_t i = 0; i < s->nb; ++i) {
+    if (s->banim[i] != 1) continue;
+    r3 p = s->bpos[i];
+    p = v3(p.x + (real)t[0], p.y + (real)t[1], p.z + (real)t[2]);
+    if (rotation_deg != 0.0f) {
+      p.x = p.x - (real)c[0];
+      p.y = p.y - (real)c[1];
+      const real nx = p.x * ct - p.y * st;
+      const real ny = p.x * st + p.y * ct;
+      p.x = nx + (real)c[0];
+      p.y = ny + (real)c[1];
+    }
+    s->bpos[i] = p;
+  }
 }
 
 /* Stand-alone grid: unsorted keys, stable sort, cell start. */

@@ -40,6 +40,7 @@ def _load(fp64: bool) -> C.CDLL:
         "error_word": (C.c_int32, [C.c_void_p]),
         "threads": (C.c_int, []),
         "destroy": (None, [C.c_void_p]),
+        "animate_walls": (None, [C.c_void_p, C.POINTER(C.c_float), C.c_float, C.POINTER(C.c_float)]),
     }
     for k, (res, args) in sig.items():
         fn = getattr(lib, pre + k)
@@ -156,6 +157,12 @@ class OracleSystem:
         if rc != 0:
             raise ValueError("oracle write failed")
 
+    def animate_walls(self, translation, rotation, center):
+        """animateParticles (main.cu:1175-1208) on the oracle's walls."""
+        t = np.ascontiguousarray(translation, np.float32)
+        c = np.ascontiguousarray(center, np.float32)
+        _fn(self._lib, "animate_walls")(self._h, _fptr(t), float(np.float32(rotation)), _fptr(c))
+
     def save_particle_stats(self, path: str):
         _fn(self._lib, "save_particle_stats")(self._h, path.encode())
 
@@ -209,3 +216,40 @@ def color_dots(pos, mass=None, surface=None, sdist=None, mode=2, min_mass=1.0, m
             special = np.array([np.float64(np.inf), 214.0 / 255.0, 160.0 / 255.0]).astype(f)
         col[m == 0] = special
     return pos.copy(), col
+
+
+def animation_advance(state: dict, dt, walls=None) -> dict:
+    """updateAnimation's decisions (main.cu:1210-1262) restated on a dict of
+    AnimationState's fields, in float32 arithmetic operation by operation.
+    Returns the frame's move: translation, rotation (degrees), center and
+    whether animateParticles runs."""
+    F = np.float32
+    dt = F(dt)
+    move = {"translation": np.zeros(3, F), "rotation": F(0), "center": np.zeros(3, F), "apply": 0}
+    if not state["is_animating"]:
+        return move
+    state["animation_time"] = F(F(state["animation_time"]) + dt)
+    tr = np.zeros(3, F)
+    rot = F(0)
+    if state["animation_time"] <= F(2.5) and not state["translation_complete"]:
+        d = np.asarray(state["translation_direction"], F)
+        tr = np.array([F(F(d[k] * F(state["translation_speed"])) * dt) for k in range(3)], F)
+    elif not state["translation_complete"]:
+        state["translation_complete"] = 1
+        state["animation_time"] = F(0)
+        cen = np.zeros(3, F)
+        count = 0
+        for i in range(state["start_index"], state["start_index"] + state["num_particles"]):
+            cen = np.array([F(cen[k] + F(walls[i][k])) for k in range(3)], F)
+            count += 1
+        if count > 0:
+            state["rotation_center"] = np.array([F(cen[k] / F(count)) for k in range(3)], F)
+    if state["translation_complete"] and F(state["rotation_angle"]) < F(45.0):
+        delta = F(-F(state["rotation_speed"]) * dt)
+        state["rotation_angle"] = F(F(state["rotation_angle"]) + abs(delta))
+        rot = delta
+        if state["rotation_angle"] >= F(45.0):
+            state["is_animating"] = 0
+    move.update(translation=tr, rotation=rot, center=np.asarray(state["rotation_center"], F).copy(),
+                apply=1 if state["is_animating"] else 0)
+    return move
