@@ -191,25 +191,40 @@ def cpu_sample(steps: int, warmup: int, fp64: bool = True):
 def fp64_error(device: int) -> dict:
     """The library (FP32, CUDA's own math functions) against the serial FP64
     restatement after one substep (the constructor's) from the same state of
-    the bounded sample: max |x - x_fp64| in units of r and max |v - v_fp64|.
-    (After a second grid build the two sort particles near cell faces
-    differently, so particles compare index by index after one substep.)"""
+    the bounded sample: max |x - x_fp64| in units of r, its 99.9th
+    percentile and the particles beyond 1e-3 r, and max |v - v_fp64|.  The
+    FP32 restatement against the FP64 one is reported beside it: with the
+    reference's wall reach (0.02 = 2.5 cells at r = 0.002) a particle near a
+    cell face sees different wall particles when a rounding moves it across
+    the face (the stencil covers one cell each way), so a few particles
+    differ by a good part of r in any FP32 build.  (After a second grid
+    build the two sort particles near cell faces differently, so particles
+    compare index by index after one substep.)"""
     import granular_gpu_gb300 as gg
     from granular_gpu_gb300 import abi, workloads
     from oracle import oracle as orc
     desc = workloads.column_collapse(counts=SAMPLE_COUNTS, constants="reference")
     s = gg.GranularSystem(**workloads.system_kwargs(desc), device=device)
     o = orc.OracleSystem(desc, fp64=True)
-    if s.size() != o.size():
-        out = {"unavailable": f"particle counts differ ({s.size()} vs {o.size()})"}
+    o32 = orc.OracleSystem(desc, fp64=False)
+    r = 0.002
+
+    def err(pos, vel):
+        d = np.abs(pos.astype(np.float64) - o.read(abi.FIELD_POS).astype(np.float64)).max(1) / r
+        dv = np.abs(vel.astype(np.float64) - o.read(abi.FIELD_VEL).astype(np.float64)).max()
+        return {"pos_max_abs_r": float(d.max()), "pos_p999_abs_r": float(np.quantile(d, 0.999)),
+                "particles_over_1e-3_r": int((d > 1e-3).sum()), "vel_max_abs": float(dv)}
+
+    if s.size() != o.size() or o32.size() != o.size():
+        out = {"unavailable": f"particle counts differ ({s.size()}, {o32.size()} vs {o.size()})"}
     else:
-        r = 0.002
-        dx = np.abs(s.read(gg.FIELD_POS).astype(np.float64) - o.read(abi.FIELD_POS).astype(np.float64)).max()
-        dv = np.abs(s.read(gg.FIELD_VEL).astype(np.float64) - o.read(abi.FIELD_VEL).astype(np.float64)).max()
-        out = {"pos_max_abs_r": float(dx / r), "vel_max_abs": float(dv), "substeps": 1,
-               "sample": "64x64x64 sub-lattice of the column scene, FP32 CUDA math against the FP64 build"}
+        out = err(s.read(gg.FIELD_POS), s.read(gg.FIELD_VEL))
+        out.update({"substeps": 1, "particles": int(o.size()),
+                    "sample": "64x64x64 sub-lattice of the column scene, FP32 CUDA math against the FP64 build",
+                    "fp32_oracle_vs_fp64": err(o32.read(abi.FIELD_POS), o32.read(abi.FIELD_VEL))})
     s.close()
     o.close()
+    o32.close()
     return out
 
 

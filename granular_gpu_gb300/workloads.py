@@ -129,10 +129,12 @@ def _desc(particles, walls, upsampled, space, L, cs, dt, g, density, adaptive, p
                 device=0, max_particles=0, params=params)
 
 
-def box_drop(n_side=32, seed=42, substeps=4, iters=3, adaptive=0, upsample_per=0, skip=False):
+def box_drop(n_side=32, seed=42, substeps=4, iters=3, adaptive=0, upsample_per=0, skip=False, configured=False):
     """Plain PBD box drop: n_side^3 unit masses, r = 0.01, lattice spacing 2r
     with uniform jitter +-0.05r, block centred 0.5 above the floor of a 1^3
-    box, dt = 1/60 split into `substeps`, `iters` Jacobi sweeps."""
+    box, dt = 1/60 split into `substeps`, `iters` Jacobi sweeps.
+    configured=True: the configuration's contact model (Coulomb friction
+    0.5 / 0.4, restitution 0, the box faces as analytic walls)."""
     r = REF_RADIUS
     L = np.float32(CELL_PER_RADIUS * r)
     space = (1.0, 1.0, 1.0)
@@ -144,6 +146,8 @@ def box_drop(n_side=32, seed=42, substeps=4, iters=3, adaptive=0, upsample_per=0
     params = scaled_params(r, iters=iters, dt_sub=None)
     params.upsample_enabled = 1 if upsample_per else 0
     params.merge_enabled = 1 if adaptive else 0
+    if configured:
+        configure(params, 0.5, 0.4, box_planes(space))
     ups = None
     if upsample_per:
         rng = np.random.default_rng(seed + 1)
@@ -220,7 +224,7 @@ def ramp_walls(space_size, cell_length, angle_deg=30.0, x0=None, x1=None):
 
 
 def adaptive_pile(counts=(64, 64, 64), r=0.005, seed=42, substeps=1, iters=5, upsample_per=4, ledger=1,
-                  max_mass=8.0, origin=None, scaled=False):
+                  max_mass=8.0, origin=None, scaled=False, configured=False):
     """The adaptive-pile configuration: fine particles of radius r in a
     jittered block at spacing 2r (64^3 = 262,144 particles fill a 0.64 m
     block: the 0.6 x 0.4 x 0.6 m block of the configuration holds only
@@ -234,7 +238,11 @@ def adaptive_pile(counts=(64, 64, 64), r=0.005, seed=42, substeps=1, iters=5, up
     as the reference would run this scene (`scaled=True` scales them by
     r / 0.01 instead).  Scaled, the wall reach drops to 2r while the wall
     particles stay half a cell apart, and a pile this tall presses most
-    particles through the one-particle-thick floor."""
+    particles through the one-particle-thick floor.
+
+    configured=True adds the configured mode: Coulomb friction 0.5 / 0.4,
+    claiming split children, and the box faces and the ramp as analytic
+    walls behind their wall particles."""
     L = np.float32(CELL_PER_RADIUS * r)
     space = (2.0, 1.0, 1.0)
     walls, cs = box_walls(space, L)
@@ -247,11 +255,25 @@ def adaptive_pile(counts=(64, 64, 64), r=0.005, seed=42, substeps=1, iters=5, up
     params = scaled_params(r if scaled else REF_RADIUS, iters=iters, dt_sub=None, max_mass=max_mass, ledger=ledger)
     params.upsample_enabled = 1 if upsample_per else 0
     params.merge_enabled = 1
+    if configured:
+        configure(params, 0.5, 0.4, box_planes(space) + [ramp_plane(space, 30.0)])
     ups = None
     if upsample_per:
         rng = np.random.default_rng(seed + 1)
         ups = (np.repeat(p, upsample_per, 0) + rng.uniform(-r, r, (p.shape[0] * upsample_per, 3))).astype(np.float32)
     return _desc(p, walls, ups, space, L, cs, dt, (0.0, -9.81, 0.0), density_for_radius(r), 1, params)
+
+
+def ramp_plane(space_size, angle_deg=30.0, x0=None):
+    """The ramp of ramp_walls as an analytic wall: y >= floor + tan(angle)
+    (x - x0).  Below x0 the half-space lies under the floor, so it binds
+    only over the ramp."""
+    sp = np.asarray(space_size, np.float64)
+    floor = 0.005 * sp[1]
+    x0 = 0.5 * sp[0] if x0 is None else x0
+    a = math.radians(angle_deg)
+    n = np.array([-math.sin(a), math.cos(a), 0.0])
+    return (n, float(n @ np.array([x0, floor, 0.0])))
 
 
 def system_kwargs(desc: dict) -> dict:

@@ -119,3 +119,59 @@ def test_configured_column_runs_200_frames():
     assert st["merged_total"] > 0 and st["split_total"] > 0, st
     assert int(st["error_word"]) == 0
     s.close()
+
+
+def _run_configured(desc, frames, substeps_per_frame, checks=4):
+    """Steps a configured scene through its frames; checks NaN, the floor,
+    the box and the mass ledger a few times on the way.  Returns the stats
+    and the particle-substeps per second of the run."""
+    import time
+    n0 = desc["n_particles"]
+    units0 = int(round(float(np.sum(desc.get("masses", np.ones(n0)), dtype=np.float64)) * abi.UNITS_PER_MASS))
+    s = gg.GranularSystem(**workloads.system_kwargs(desc), device=0)
+    sp = np.asarray(desc["space_size"], np.float32)
+    lo, hi = 0.005 * sp, 0.995 * sp
+    every = max(1, frames // checks)
+    work = 0
+    t0 = time.perf_counter()
+    for frame in range(frames):
+        work += s.size() * substeps_per_frame
+        s.step(substeps_per_frame)
+        if frame % every == every - 1 or frame == frames - 1:
+            st = s.stats()
+            assert st["nonfinite"] == 0, f"frame {frame}: NaN positions"
+            assert st["total_mass_units"] == units0, f"frame {frame}: mass units"
+            p = s.read(gg.FIELD_POS)
+            assert np.all(p >= lo) and np.all(p <= hi), \
+                f"frame {frame}: {int(np.sum(np.any((p < lo) | (p > hi), 1)))} particles outside the box"
+    s.synchronize()
+    rate = work / (time.perf_counter() - t0)
+    st = s.stats()
+    s.close()
+    return st, rate
+
+
+def test_box_drop_configuration_300_frames():
+    # 32^3 particles, r = 0.01, dt = 1/60 in 4 substeps, 3 Jacobi sweeps,
+    # friction 0.5 / 0.4, restitution 0: 300 frames
+    st, rate = _run_configured(workloads.box_drop(n_side=32, substeps=4, iters=3, configured=True), 300, 4)
+    print(f"box drop 32^3: {rate / 1e6:.1f} M particle-substeps/s (with the checks)")
+    assert int(st["error_word"]) == 0
+
+
+def test_adaptive_pile_configuration_600_frames():
+    # 262,144 particles (r = 0.005) onto the floor and the 30-degree ramp,
+    # merge/split up to mass 8, 4 render points each, dt = 1/240: 600 frames
+    st, rate = _run_configured(workloads.adaptive_pile(configured=True), 600, 1)
+    print(f"adaptive pile 262k: {rate / 1e6:.1f} M particle-substeps/s (with the checks)")
+    assert st["merged_total"] > 0 and int(st["error_word"]) == 0
+
+
+def test_column_collapse_configuration_200_frames_at_full_size():
+    # 8,388,608 particles (r = 0.002), 33,554,432 render points, dt = 1/120
+    # in 4 substeps, 4 Jacobi sweeps, merge/split up to mass 8: 200 frames
+    desc = workloads.column_collapse(counts=(128, 256, 256), constants="configured")
+    assert desc["n_particles"] == 8_388_608
+    st, rate = _run_configured(desc, 200, 4)
+    print(f"column collapse 8.4M: {rate / 1e6:.1f} M particle-substeps/s (with the checks)")
+    assert st["merged_total"] > 0 and st["split_total"] > 0 and int(st["error_word"]) == 0
