@@ -47,7 +47,8 @@ SAMPLE_NOTE = "64x64x64 sub-lattice (262,144 particles) of the same column scene
 # float3 state and neighbour re-reads assumed to hit in cache: the roofline
 # is reported for whichever class takes the most time in the timed region.
 ALGO_BYTES = {
-    "sweep": (28, "particle", "read x* and radius 16 B, write x* 12 B"),
+    "sweep": (40, "particle", "read x* and contact radius 16 B, inverse mass 4 B and cell key 4 B; write the "
+                              "correction and its counts 16 B"),
     "upsample": (48, "render point", "read render-point position and velocity 24 B, write them 24 B"),
     "surface": (20, "particle", "read position and radius 16 B, write the surface flag 4 B"),
     "apply": (56, "particle", "read correction 16 B and x* 12 B, write x* 12 B (stabilisation: x 12 B more), "
