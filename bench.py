@@ -501,13 +501,18 @@ def run_mine(args):
     t0 = time.perf_counter()
     e2e_units = 0
     h2d = d2h = 0
+    step_evs = []
     for _ in range(args.steps_e2e):
         # this step's inputs from the host, the step, its results back
         sysg.write(gg.FIELD_POS, hp_all[:m])
         sysg.write(gg.FIELD_VEL, hv_all[:m])
         h2d += 2 * 12 * m
         e2e_units += m
+        ea, eb = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ea.record(stream)
         sysg.step(1)
+        eb.record(stream)
+        step_evs.append((ea, eb))
         m = sysg.size()
         sysg.read(gg.FIELD_POS, out=hp_all[:m])
         sysg.read(gg.FIELD_VEL, out=hv_all[:m])
@@ -517,6 +522,9 @@ def run_mine(args):
     e2e_s = time.perf_counter() - t0
     e2e_s_max, e2e_total = reduce_over_ranks(e2e_s, e2e_units)
     e2e_value = e2e_total / e2e_s_max if args.steps_e2e else None
+    # the same substeps' device time alone (CUDA events around each step on
+    # the library's stream): what the copies and the host add is the rest
+    e2e_step_ms = sum(a.elapsed_time(b) for a, b in step_evs)
 
     # ---- roofline of the dominant kernel class
     known = {k: v for k, v in prof.items() if k in ALGO_BYTES and v["launches"]}
@@ -551,7 +559,12 @@ def run_mine(args):
                      "list_builds_per_particle_sweep": list_builds / max(prof["sweep"]["units"], 1),
                      "stream_kernels": stream_kernels(prof, desc, peak)},
         "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d // max(args.steps, 1),
-                "d2h_bytes_per_step": d2h // max(args.steps, 1)},
+                "d2h_bytes_per_step": d2h // max(args.steps, 1),
+                "ms_per_step": e2e_s_max * 1e3 / max(args.steps_e2e, 1),
+                "device_ms_per_step": e2e_step_ms / max(args.steps_e2e, 1),
+                "device_only_value": (e2e_units / (e2e_step_ms / 1e3)) if args.steps_e2e and e2e_step_ms > 0
+                else None,
+                "substeps": f"{WINDOW_START + args.steps}..{WINDOW_START + 2 * args.steps - 1}"},
         "gpu_launches": int(launches),
         "clocks": clocks,
         "early_window": early,
