@@ -45,7 +45,7 @@ struct SweepArgs {
   double brad;   // boundary radius (double literal 0.01)
   double fcap;   // friction cap (double literal 0.8)
   float minr;    // floor of the particle radius against walls (0.01f)
-  // contact candidate lists (variant 5)
+  // contact candidate lists (the default sweep)
   int32_t* __restrict__ nl_idx;
   int4* __restrict__ nl_meta;
   float* __restrict__ nl_acc;
@@ -342,17 +342,15 @@ __global__ void __launch_bounds__(256) k_sweep(SweepArgs a) {
   sweep_global<MM>(a, i, t);
 }
 
-// ------------------------------------------------------------ warp sweep
+// ------------------------------------------------------------ listed scan
 //
 // The reference sums a particle's corrections over its 27 cells in the
 // order m = (dx+1)*9 + (dy+1)*3 + (dz+1) and, inside a cell, walls then
-// particles by index.  Because the cell key is lexicographic in (x, y, z),
-// that order is increasing cell key, and particles are stored by key: a
-// lane's reference order is increasing key, walls before particles of the
-// same cell.  A warp therefore visits the union of its lanes' stencils in
-// key order, every candidate loaded once for the whole warp; each lane keeps
-// the candidates that pass a cheap distance test in a list (in order), and
-// the lanes then process their k-th listed candidate together.
+// particles by index.  Without contact lists (nlist_skin = 0) each lane
+// walks its 27 cells in that order and keeps the candidates that pass a
+// cheap distance test in a short list in shared memory (in order); the
+// lanes then run the exact test on their k-th listed candidate together,
+// which keeps the expensive contact body convergent across the warp.
 
 constexpr int kWarpList = 32;      // listed candidates per lane before a flush
 constexpr int kWarpThreads = 256;
