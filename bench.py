@@ -605,12 +605,14 @@ def run_mine(args):
                 "residual": f"mean penetration over contacts <= {tol:g} r, checked before every Jacobi sweep "
                             f"(cap {cap} sweeps; a capped plain frame stops short, which favours the plain solver)",
                 "scene": f"block 0.6x0.4x0.6 of {sc['particles']} particles (r=0.005, spacing 2r) dropped 0.02 onto "
-                         f"the floor, held-out seed {sc['seed']}, {frames} substeps of 1/240 s"}
+                         f"the floor, Coulomb friction 0.5 / 0.4, held-out seed {sc['seed']}, {frames} substeps "
+                         f"of 1/240 s"}
         mlp.close()
         line["learned_warm_start"] = dict(runs[1e-3])
         line["learned_warm_start"]["at_1e-2_r"] = runs[1e-2]
         line["learned_warm_start"]["network"] = ("48-64-64-3 MLP, BF16 tcgen05 kernels, trained on 2,000 solver frames "
-                                                 "solved to 1e-3 r (granular_gpu_gb300/weights/warm_start_mlp.npy)")
+                                                 "solved to 1e-3 r, Coulomb friction drawn U[0.3, 0.7] "
+                                                 "(granular_gpu_gb300/weights/warm_start_mlp.npy)")
     if rank == 0 and world == 1 and not args.no_cpu:
         cv, threads, _ = cpu_sample(steps=args.cpu_steps, warmup=1)
         line["cpu_baseline"] = {"value": cv, "unit": METRIC, "cores": threads, "kind": "port",

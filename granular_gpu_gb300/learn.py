@@ -4,15 +4,18 @@ the library's tensor-core kernels, and the time-to-residual evaluation.
 Scenes follow the adaptive-pile configuration's style without merge/split or
 upsampling: a jittered block of particles of radius r = 0.005 (lattice
 spacing 2r) released just above the floor of a box, substeps of dt = 1/240,
-3 stabilisation sweeps and then Jacobi sweeps until the mean penetration
-over contacts is at most 1e-3 r (gg_params.target_residual), or a cap on the
-sweeps is reached.  A frame is one substep.  `python -m
-granular_gpu_gb300.learn train` (defaults: 8 scenes of 250 frames solved to
-1e-3 r with at most 2,000 sweeps a frame) makes the shipped weights.
-The network is trained on the correction the plain sweeps reach in each
-frame (recorded by the library with gg_params.warm_start = 2) and evaluated
-on held-out seeds by Jacobi sweeps and device time to the same residual,
-with and without the warm start, from the same initial state.
+Coulomb friction with a static coefficient drawn U[0.3, 0.7] (the configured
+mode: kinetic 0.8 of it, the box faces as analytic walls), and Jacobi sweeps
+until the mean penetration over contacts is at most 1e-3 r
+(gg_params.target_residual), or a cap on the sweeps is reached.  A frame is
+one substep.  `python -m granular_gpu_gb300.learn train` (defaults: 8
+scenes of 250 frames solved to 1e-3 r with at most 2,000 sweeps a frame)
+makes the shipped weights.  The network is trained on the correction the
+plain sweeps reach in each frame (recorded by the library with
+gg_params.warm_start = 2) and evaluated on held-out seeds by Jacobi sweeps
+and device time to the same residual, with and without the warm start,
+from the same initial state.  `--law cap` runs the same with the
+reference's contact law instead (friction as its tangential cap).
 """
 import math
 import os
@@ -28,9 +31,14 @@ TOL = 1e-3 * R
 
 
 def pile_scene(seed: int, dims=(0.5, 0.5, 0.5), friction_cap: float = 0.5, r: float = R, drop: float = 0.02,
-               target_residual: float = TOL, max_sweeps: int = 200, warm_start: int = 0, scale: float = 1.0):
+               target_residual: float = TOL, max_sweeps: int = 200, warm_start: int = 0, scale: float = 1.0,
+               law: str = "coulomb"):
     """A jittered block (dims in metres, spacing 2r, jitter +-0.05r) centred
-    in a box and released `drop` above the floor walls."""
+    in a box and released `drop` above the floor walls.  law="coulomb" (the
+    default): the configured mode's Coulomb friction with mu_static =
+    `friction_cap` and mu_kinetic = 0.8 of it, the box faces as analytic
+    walls, Jacobi sweeps only; law="cap": the reference's contact law with
+    `friction_cap` as its tangential cap, 3 stabilisation sweeps first."""
     L = np.float32(workloads.CELL_PER_RADIUS * r)
     counts = [max(2, int(round(d / (2 * r)))) for d in dims]
     side = max(1.0, 1.2 * max(counts[0], counts[2]) * 2 * r)
@@ -49,14 +57,19 @@ def pile_scene(seed: int, dims=(0.5, 0.5, 0.5), friction_cap: float = 0.5, r: fl
     params.max_sweeps = int(max_sweeps)
     params.warm_start = int(warm_start)
     params.warm_start_scale = float(scale)
+    if law == "coulomb":
+        workloads.configure(params, friction_cap, 0.8 * friction_cap, workloads.box_planes(space))
+    elif law != "cap":
+        raise ValueError(law)
     desc = workloads._desc(p, walls, None, space, L, cs, DT, (0.0, -9.81, 0.0), workloads.density_for_radius(r),
                            0, params, skip=True)
     return desc
 
 
 def draw_scene(rng, **kw):
-    """Block dimensions U[0.3, 0.8] m and friction U[0.3, 0.7] (the
-    friction cap of the contact kernel, 0.8 in the reference)."""
+    """Block dimensions U[0.3, 0.8] m and friction U[0.3, 0.7] (the static
+    Coulomb coefficient; with law="cap" the contact kernel's friction cap,
+    0.8 in the reference)."""
     dims = tuple(float(rng.uniform(0.3, 0.8)) for _ in range(3))
     return pile_scene(int(rng.integers(1 << 30)), dims=dims, friction_cap=float(rng.uniform(0.3, 0.7)), **kw)
 
@@ -159,14 +172,15 @@ def load_mlp(path: str = WEIGHTS, device: int = 0) -> Mlp:
 
 
 def evaluate(mlp: Mlp, seeds=(101, 102), frames: int = 150, dims=EVAL_DIMS, tol: float = 1e-2,
-             friction_cap: float = 0.5, device: int = 0, max_sweeps: int = 250) -> dict:
+             friction_cap: float = 0.5, device: int = 0, max_sweeps: int = 250, law: str = "coulomb") -> dict:
     """Plain vs warm-started residual-mode runs of held-out scenes from the
     same initial state: device ms and Jacobi sweeps summed over the frames,
     and the frames that reached the residual within the sweep cap."""
     out = {"tolerance_r": tol, "frames": frames, "max_sweeps": max_sweeps, "scenes": []}
     tp = tl = sp = sl = 0.0
     for seed in seeds:
-        d = pile_scene(seed, dims=dims, friction_cap=friction_cap, target_residual=tol * R, max_sweeps=max_sweeps)
+        d = pile_scene(seed, dims=dims, friction_cap=friction_cap, target_residual=tol * R, max_sweeps=max_sweeps,
+                       law=law)
         msp, swp, rp = run_scene(d, frames, device=device)
         msl, swl, rl = run_scene(d, frames, mlp=mlp, device=device)
         out["scenes"].append({"seed": seed, "particles": d["n_particles"], "plain_ms": float(msp.sum()),
@@ -204,10 +218,14 @@ def main(argv=None):
     ap.add_argument("--weights", default=WEIGHTS)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--eval-seeds", default="101,102")
+    ap.add_argument("--law", choices=["cap", "coulomb"], default="coulomb",
+                    help="contact law of the scenes: Coulomb friction (configured mode), or the reference's "
+                         "friction cap")
     a = ap.parse_args(argv)
     if a.cmd == "train":
         rng = np.random.default_rng(a.seed)
-        descs = [draw_scene(rng, target_residual=a.tol * R, max_sweeps=a.max_sweeps) for _ in range(a.scenes)]
+        descs = [draw_scene(rng, target_residual=a.tol * R, max_sweeps=a.max_sweeps, law=a.law)
+                 for _ in range(a.scenes)]
         t0 = time.time()
         X, T = collect(descs, frames=a.frames, per_frame=a.per_frame, seed=a.seed)
         t1 = time.time()
@@ -224,7 +242,7 @@ def main(argv=None):
     elif a.cmd == "evaluate":
         m = load_mlp(a.weights)
         seeds = tuple(int(s) for s in a.eval_seeds.split(","))
-        print(json.dumps(evaluate(m, seeds=seeds, frames=a.frames, tol=a.tol, max_sweeps=a.max_sweeps)))
+        print(json.dumps(evaluate(m, seeds=seeds, frames=a.frames, tol=a.tol, max_sweeps=a.max_sweeps, law=a.law)))
     else:
         print(json.dumps(bench_kernels(a.rows, seed=a.seed)))
     return 0
