@@ -383,6 +383,51 @@ def pile_rate(device: int, steps: int) -> dict:
                         "and timed after 100 substeps"}
 
 
+def box_drop_rate(device: int) -> dict:
+    """The box-drop configuration as stated (configured mode): 32^3
+    particles, r = 0.01, dt = 1/60 in 4 substeps, 3 Jacobi sweeps, Coulomb
+    friction 0.5 / 0.4, restitution 0, box faces as analytic walls; all 300
+    frames timed (device time, CUDA events), stepped substep by substep and,
+    from the same start, each frame's 4 substeps replayed as one CUDA graph
+    (the scene has no merge/split, so a frame needs no host round trip)."""
+    import torch
+    import granular_gpu_gb300 as gg
+    from granular_gpu_gb300 import workloads
+    frames = 300
+    out = {}
+    for mode in ("stepped", "graph"):
+        desc = workloads.box_drop(n_side=32, substeps=4, iters=3, configured=True)
+        s = gg.GranularSystem(**workloads.system_kwargs(desc), device=device)
+        if mode == "graph":
+            s.graph_capture(4)
+        st = torch.cuda.ExternalStream(s.stream, device=device)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(frames):
+            if mode == "graph":
+                s.graph_launch()
+            else:
+                s.step(4)
+        e1.record(st)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        stats = s.stats()
+        p = s.read(gg.FIELD_POS)
+        out[mode] = {"ms": ms, "nonfinite": stats["nonfinite"], "pos": p}
+        s.close()
+    n = desc["n_particles"]
+    g, t = out["graph"], out["stepped"]
+    return {"metric": METRIC, "value": n * 4 * frames / (g["ms"] / 1e3), "ms_per_frame": g["ms"] / frames,
+            "stepped_value": n * 4 * frames / (t["ms"] / 1e3), "stepped_ms_per_frame": t["ms"] / frames,
+            "graph_equals_stepping": bool(np.array_equal(g["pos"], t["pos"])),
+            "frames": frames, "substeps": 4 * frames, "particles": n, "nonfinite": g["nonfinite"],
+            "inside_box": bool(np.all(g["pos"] >= 0.005) and np.all(g["pos"] <= 0.995)),
+            "workload": "32^3 box drop (r = 0.01, lattice 2r, jitter 0.05r, block centred 0.5 above the floor), "
+                        "dt = 1/60 in 4 substeps, 3 Jacobi sweeps, Coulomb friction 0.5 / 0.4, restitution 0, "
+                        "box faces as analytic walls (configured mode), 300 frames from rest, each frame one "
+                        "CUDA-graph launch"}
+
+
 def scaled_rate(device: int, counts, warmup: int, steps: int) -> dict:
     """The same column with every length constant scaled by r / 0.01 (a
     configuration of this library the reference's compiled-in constants
@@ -581,6 +626,9 @@ def run_mine(args):
         # integer ledger, 4 render points per particle; timed after 100
         # substeps (merges under way)
         line["adaptive_pile"] = pile_rate(local, args.pile_steps)
+    if rank == 0 and world == 1 and not args.no_pile:
+        # the box-drop configuration as stated (Coulomb friction 0.5 / 0.4)
+        line["box_drop_configured"] = box_drop_rate(local)
     if rank == 0 and world == 1 and not args.no_batched:
         # batched scenes: 64 scenes in one system, autotuned, replayed as a
         # CUDA graph, against the same scenes stepped one after another

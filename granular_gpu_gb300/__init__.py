@@ -349,6 +349,16 @@ class GranularSystem:
         _check(lib().gg_frame_times(self._h, _fptr(out), out.shape[0], C.byref(n)))
         return out[:n.value]
 
+    def graph_capture(self, substeps: int):
+        """Records `substeps` substeps (an even number) into a CUDA graph
+        (gg_graph_capture); only for substeps without host round trips (no
+        merge/split, no residual mode)."""
+        _check(lib().gg_graph_capture(self._h, int(substeps)))
+
+    def graph_launch(self):
+        """Replays the captured substeps with one launch (gg_graph_launch)."""
+        _check(lib().gg_graph_launch(self._h))
+
     def update_animation(self, state: "abi.gg_animation", dt: float):
         """updateAnimation (main.cu:1210-1277): advances `state` by one frame
         of dt and moves the animated walls (before the frame's substeps)."""
