@@ -253,6 +253,7 @@ SIGNATURES = {
     "gg_get_params": (C.c_int, [P_, C.POINTER(gg_params)]),
     "gg_set_scenes": (C.c_int, [P_, C.c_int32, C.c_float, C.POINTER(C.c_float)]),
     "gg_scene_stats": (C.c_int, [P_, C.POINTER(C.c_double), C.c_int32]),
+    "gg_set_scene_coulomb": (C.c_int, [P_, C.c_int32, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     "gg_graph_capture": (C.c_int, [P_, C.c_int32]),
     "gg_graph_launch": (C.c_int, [P_]),
     "gg_autotune": (C.c_int, [P_, C.c_int32, C.POINTER(gg_tuning)]),

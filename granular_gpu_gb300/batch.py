@@ -2,7 +2,11 @@
 
 The batched-scenes configuration: 64 box-drop / pile scenes with particle
 counts drawn log-uniform in [10,000, 500,000] (seeded), radius 0.005,
-friction U[0.3, 0.7], stepped together.  Scene k sits in the slab
+friction U[0.3, 0.7], stepped together.  law="coulomb" (the default) runs
+the configured mode with the friction as each scene's static Coulomb
+coefficient (kinetic 0.8 of it) and its box faces as analytic walls in the
+scene's own coordinates; law="cap" runs the reference's contact law with the
+friction as each scene's tangential cap.  Scene k sits in the slab
 k*W <= x < (k+1)*W (W = its 1 m box plus a gap of two cells), so one grid,
 one sort and one launch of each kernel serve all scenes and no contact
 crosses scenes (gg_set_scenes); a frame of substeps is captured once into a
@@ -33,9 +37,10 @@ def _scene(rng, n: int, r: float = R):
     return p
 
 
-def batched_scenes(n_scenes: int = 64, seed: int = 0, lo: int = 10_000, hi: int = 500_000, r: float = R):
+def batched_scenes(n_scenes: int = 64, seed: int = 0, lo: int = 10_000, hi: int = 500_000, r: float = R,
+                   law: str = "coulomb"):
     """(desc, info) of a batch: desc for GranularSystem(...); info holds the
-    slab width, per-scene friction caps and particle ranges."""
+    slab width, per-scene friction and particle ranges."""
     rng = np.random.default_rng(seed)
     L = np.float32(workloads.CELL_PER_RADIUS * r)
     counts = np.exp(rng.uniform(math.log(lo), math.log(hi), n_scenes)).astype(np.int64)
@@ -56,10 +61,14 @@ def batched_scenes(n_scenes: int = 64, seed: int = 0, lo: int = 10_000, hi: int 
     params = workloads.scaled_params(r, iters=5)
     params.upsample_enabled = 0
     params.merge_enabled = 0
+    if law == "coulomb":
+        workloads.configure(params, 0.5, 0.4, workloads.box_planes((BOX, BOX, BOX)))
+    elif law != "cap":
+        raise ValueError(law)
     desc = workloads._desc(particles, boundary, None, space, L, cell_size, DT, (0.0, -9.81, 0.0),
                            workloads.density_for_radius(r), 0, params, skip=True)
     info = {"n_scenes": n_scenes, "width": W, "friction_cap": fric, "sizes": np.array(sizes),
-            "walls_per_scene": walls1.shape[0]}
+            "walls_per_scene": walls1.shape[0], "law": law}
     return desc, info
 
 
@@ -77,6 +86,9 @@ def scene_desc(desc, info, k: int):
     params = abi.gg_params()
     C.memmove(C.byref(params), C.byref(desc["params"]), C.sizeof(params))
     params.friction_cap = float(info["friction_cap"][k])
+    if info.get("law") == "coulomb":
+        params.mu_static = float(info["friction_cap"][k])
+        params.mu_kinetic = float(np.float32(0.8) * info["friction_cap"][k])
     return workloads._desc(p, w, None, (BOX, BOX, BOX), L, cs, desc["dt"], desc["gravity"], desc["density"], 0,
                            params, skip=True)
 
@@ -91,6 +103,13 @@ class Batch:
         fc = np.ascontiguousarray(info["friction_cap"], np.float32)
         _check(lib().gg_set_scenes(self.system._h, info["n_scenes"], info["width"],
                                    fc.ctypes.data_as(C.POINTER(C.c_float))))
+        if info.get("law") == "coulomb":
+            mus = fc
+            muk = np.ascontiguousarray(np.float32(0.8) * fc, np.float32)
+            self._mu = (mus, muk)
+            _check(lib().gg_set_scene_coulomb(self.system._h, info["n_scenes"],
+                                              mus.ctypes.data_as(C.POINTER(C.c_float)),
+                                              muk.ctypes.data_as(C.POINTER(C.c_float))))
 
     def scene_stats(self) -> np.ndarray:
         """n_scenes x 9: count, mass, momentum xyz, kinetic energy, centre of mass xyz (FP64)."""
@@ -114,7 +133,7 @@ class Batch:
 
 
 def measure(n_scenes: int = 64, frames: int = 10, substeps: int = 4, seed: int = 0, device: int = 0,
-            sequential: bool = True) -> dict:
+            sequential: bool = True, law: str = "coulomb") -> dict:
     """Aggregate particle-substeps/s of the batch replayed as a CUDA graph
     (one launch per frame of `substeps` substeps), of the same batch stepped
     substep by substep, and of the scenes as separate systems stepped one
@@ -122,10 +141,11 @@ def measure(n_scenes: int = 64, frames: int = 10, substeps: int = 4, seed: int =
     the same initial state, runs one untimed frame, then `frames` timed
     frames; device time with CUDA events on the stream it runs on."""
     import torch
-    desc, info = batched_scenes(n_scenes, seed=seed)
+    desc, info = batched_scenes(n_scenes, seed=seed, law=law)
     n_total = int(desc["n_particles"])
     units = n_total * substeps * frames
     out = {"scenes": n_scenes, "particles": n_total, "frames": frames, "substeps_per_frame": substeps,
+           "contact_law": law,
            "boundary_particles": int(desc["n_boundary"]), "cells": int(np.prod(desc["cell_size"]))}
 
     def timed(stream, fn):

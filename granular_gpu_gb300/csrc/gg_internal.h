@@ -212,6 +212,7 @@ struct gg_system {
   int n_scenes = 0;
   float scene_width = 0.0f;
   float* scene_fcap = nullptr;         // device, per scene
+  float2* scene_mu = nullptr;          // device, per scene: Coulomb mu_static, mu_kinetic
   double* scene_acc = nullptr;         // device, per scene x kSceneStats
   // a captured substep sequence (gg_graph_capture)
   cudaGraphExec_t graph_exec = nullptr;

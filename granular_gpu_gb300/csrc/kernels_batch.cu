@@ -72,8 +72,10 @@ gg_status gg_set_scenes(gg_system* S, int32_t n_scenes, float width, const float
   GG_CUDA(cudaStreamSynchronize(S->stream));
   cudaFree(S->scene_fcap);
   cudaFree(S->scene_acc);
+  cudaFree(S->scene_mu);
   S->scene_fcap = nullptr;
   S->scene_acc = nullptr;
+  S->scene_mu = nullptr;
   S->n_scenes = 0;
   S->scene_width = 0.0f;
   if (n_scenes == 0) return GG_OK;
@@ -84,6 +86,30 @@ gg_status gg_set_scenes(gg_system* S, int32_t n_scenes, float width, const float
   }
   S->n_scenes = n_scenes;
   S->scene_width = width;
+  return GG_OK;
+}
+
+gg_status gg_set_scene_coulomb(gg_system* S, int32_t n_scenes, const float* mu_static, const float* mu_kinetic) {
+  if (!S || n_scenes != S->n_scenes || n_scenes <= 0 || !mu_static != !mu_kinetic) {
+    set_error("gg_set_scene_coulomb: set the scenes first (gg_set_scenes), pass their number and both "
+              "coefficient arrays (or neither)");
+    return GG_ERR_INVALID_ARGUMENT;
+  }
+  GG_CUDA(cudaSetDevice(S->device));
+  GG_CUDA(cudaStreamSynchronize(S->stream));
+  cudaFree(S->scene_mu);
+  S->scene_mu = nullptr;
+  if (!mu_static) return GG_OK;
+  std::vector<float2> mu((size_t)n_scenes);
+  for (int k = 0; k < n_scenes; ++k) {
+    if (!(mu_static[k] >= 0.0f) || !(mu_kinetic[k] >= 0.0f)) {
+      set_error("gg_set_scene_coulomb: coefficients must be non-negative");
+      return GG_ERR_INVALID_ARGUMENT;
+    }
+    mu[k] = make_float2(mu_static[k], mu_kinetic[k]);
+  }
+  GG_CUDA(cudaMalloc((void**)&S->scene_mu, sizeof(float2) * n_scenes));
+  GG_CUDA(cudaMemcpy(S->scene_mu, mu.data(), sizeof(float2) * n_scenes, cudaMemcpyHostToDevice));
   return GG_OK;
 }
 

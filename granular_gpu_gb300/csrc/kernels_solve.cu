@@ -83,6 +83,11 @@ struct PlaneArgs {
   int coulomb;    // contact_law 1
   float mus, muk;
   float4 pl[8];   // unit normal, offset: a particle keeps n . x >= d + r
+  // batched scenes: walls in scene coordinates (x - s W for scene s, the
+  // slab floor(x / W)) and, when given, Coulomb coefficients per scene
+  int n_scenes;
+  float scene_w, scene_inv_w;
+  const float2* __restrict__ scene_mu;
 };
 
 // change_position_functor (Solver.cu:403-414): x* += delta / max(1, n); in
@@ -98,6 +103,8 @@ struct PlaneArgs {
 // whole while its length is below mu_static times the normal correction the
 // particle received in this substep so far (pn: the averaged contact
 // corrections and the wall projections), else cut to mu_kinetic times it.
+// In a batch of scenes the walls are in each scene's own coordinates and
+// the coefficients those of the particle's scene.
 __global__ void __launch_bounds__(256) k_apply(int n, float4* __restrict__ xs, float4* __restrict__ pos,
                         const float4* __restrict__ delta, int32_t* __restrict__ s_extra,
                         int32_t* __restrict__ ncon, int32_t* __restrict__ contacts, int stab, int last,
@@ -132,9 +139,21 @@ __global__ void __launch_bounds__(256) k_apply(int n, float4* __restrict__ xs, f
     }
     float pni = 0.0f;
     if (fdelta) pni = pn[i] + len3(inc);
+    float mus = pa.mus, muk = pa.muk, xoff = 0.0f;
+    if (pa.n_scenes > 0) {
+      const int sc = min(max(__float2int_rz(x.x * pa.scene_inv_w), 0), pa.n_scenes - 1);
+      xoff = (float)sc * pa.scene_w;
+      if (pa.scene_mu) {
+        const float2 mu = pa.scene_mu[sc];
+        mus = mu.x;
+        muk = mu.y;
+      }
+    }
+    // a wall's offset in this particle's scene
+    auto wall_d = [&](int k) { return pa.n_scenes > 0 ? pa.pl[k].w + pa.pl[k].x * xoff : pa.pl[k].w; };
     for (int k = 0; k < pa.n; ++k) {
       const float3 nrm = make_float3(pa.pl[k].x, pa.pl[k].y, pa.pl[k].z);
-      const float sd = dot3(nrm, f3(x)) - pa.pl[k].w - x.w;
+      const float sd = dot3(nrm, f3(x)) - wall_d(k) - x.w;
       if (!(sd < 0.0f)) continue;
       x.x = x.x + -sd * nrm.x;
       x.y = x.y + -sd * nrm.y;
@@ -154,7 +173,7 @@ __global__ void __launch_bounds__(256) k_apply(int n, float4* __restrict__ xs, f
       if (fc > 0) {
         const float3 ft = div3s(make_float3(fd.x, fd.y, fd.z), (float)fc);
         const float lt = len3(ft);
-        const float f = lt < pa.mus * pni ? 1.0f : fminf(pa.muk * pni / lt, 1.0f);
+        const float f = lt < mus * pni ? 1.0f : fminf(muk * pni / lt, 1.0f);
         x.x = x.x + f * ft.x;
         x.y = x.y + f * ft.y;
         x.z = x.z + f * ft.z;
@@ -164,12 +183,12 @@ __global__ void __launch_bounds__(256) k_apply(int n, float4* __restrict__ xs, f
       // projection
       for (int k = 0; k < pa.n; ++k) {
         const float3 nrm = make_float3(pa.pl[k].x, pa.pl[k].y, pa.pl[k].z);
-        const float sd = dot3(nrm, f3(x)) - pa.pl[k].w - x.w;
+        const float sd = dot3(nrm, f3(x)) - wall_d(k) - x.w;
         if (!(sd < 0.01f * x.w)) continue;
         const float3 drel = sub3(f3(x), f3(p));
         const float3 tn = sub3(drel, smul3(dot3(drel, nrm), nrm));
         const float lt = len3(tn);
-        const float f = lt < pa.mus * pni ? 1.0f : fminf(pa.muk * pni / lt, 1.0f);
+        const float f = lt < mus * pni ? 1.0f : fminf(muk * pni / lt, 1.0f);
         x.x = x.x - f * tn.x;
         x.y = x.y - f * tn.y;
         x.z = x.z - f * tn.z;
@@ -219,6 +238,10 @@ gg_status apply(gg_system* S, int it, bool stab, bool last, cudaStream_t st) {
   pa.muk = S->P.mu_kinetic;
   for (int k = 0; k < 8; ++k)
     pa.pl[k] = make_float4(S->P.planes[k][0], S->P.planes[k][1], S->P.planes[k][2], S->P.planes[k][3]);
+  pa.n_scenes = S->n_scenes;
+  pa.scene_w = S->scene_width;
+  pa.scene_inv_w = S->scene_width > 0.0f ? 1.0f / S->scene_width : 0.0f;
+  pa.scene_mu = S->scene_mu;
   const int ta = S->tune.apply_threads;
   k_apply<<<blocks_for(S->n, ta), ta, 0, st>>>((int)S->n, S->g.xs, S->g.pos[S->g.cur], S->g.delta,
                                                  S->g.s_extra, S->g.ncon, S->g.contacts, stab ? 1 : 0,

@@ -216,7 +216,7 @@ static void free_all(gg_system* S) {
                   G.split_slot, G.keep_slot, G.child_pos, G.nl_idx, G.nl_meta, G.nl_acc, G.nl_queue, G.cell_inc, G.ld_sum, G.ld_cnt, G.claim_tgt, G.claimed, G.cell_claim, G.child_cell, G.fdelta, G.pn, S->b.pos, S->b.animated, S->b.pos_alt,
                   S->b.animated_alt, S->b.keys, S->b.perm, S->b.cell_start, S->u.keys, S->u.perm, S->scal,
                   S->stats_partial, S->stage, S->feat, S->xs0, S->warm_target, S->scene_fcap,
-                  S->scene_acc};
+                  S->scene_acc, S->scene_mu};
   for (void* p : ptrs) cudaFree(p);
   if (S->scal_host) cudaFreeHost(S->scal_host);
   sort_scratch_free(S->sort);

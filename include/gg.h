@@ -488,8 +488,14 @@ gg_status gg_grid_build_noalloc(int32_t device, const float* d_pos, int64_t n,
  * step every scene.
  */
 /* Declares the slabs; friction_cap (optional, n_scenes values) replaces
- * gg_params.friction_cap per scene. */
+ * gg_params.friction_cap per scene.  With slabs declared, the analytic
+ * walls of gg_params.planes are in each scene's own coordinates (x less
+ * k*width for scene k). */
 gg_status gg_set_scenes(gg_system* sys, int32_t n_scenes, float width, const float* friction_cap);
+/* Configured mode in a batch: Coulomb coefficients per scene (n_scenes
+ * values each, after gg_set_scenes with the same n_scenes), replacing
+ * gg_params.mu_static / mu_kinetic; NULL for both clears them. */
+gg_status gg_set_scene_coulomb(gg_system* sys, int32_t n_scenes, const float* mu_static, const float* mu_kinetic);
 /* FP64 per-scene diagnostics, 9 doubles per scene: particle count, mass,
  * momentum x y z, kinetic energy, centre of mass x y z. */
 gg_status gg_scene_stats(gg_system* sys, double* host_out, int32_t n_scenes);

@@ -9,8 +9,11 @@ from granular_gpu_gb300 import batch as B, workloads
 pytestmark = pytest.mark.gpu
 
 
-def test_batch_of_one_scene_equals_the_scene_alone():
-    desc, info = B.batched_scenes(1, seed=3, lo=3000, hi=6000)
+@pytest.mark.parametrize("law", ["coulomb", "cap"])
+def test_batch_of_one_scene_equals_the_scene_alone(law):
+    # Coulomb friction per scene (configured mode, the box faces as walls in
+    # the scene's coordinates) or the reference's law with a cap per scene
+    desc, info = B.batched_scenes(1, seed=3, lo=3000, hi=6000, law=law)
     b = B.Batch(desc, info)
     s = gg.GranularSystem(**workloads.system_kwargs(B.scene_desc(desc, info, 0)), device=0)
     b.system.step(30)
@@ -96,3 +99,27 @@ def test_autotune_restores_the_state_and_keeps_results():
     assert np.array_equal(a.system.read(gg.FIELD_POS), c.system.read(gg.FIELD_POS))
     a.close()
     c.close()
+
+
+def test_coulomb_walls_and_coefficients_follow_each_scene():
+    # two scenes, the second one slab over: the walls of gg_params.planes
+    # hold each scene's particles inside its own box, and the per-scene
+    # coefficients are the scenes' own (stepping each alone agrees)
+    desc, info = B.batched_scenes(2, seed=8, lo=2000, hi=4000, law="coulomb")
+    b = B.Batch(desc, info)
+    alone = [gg.GranularSystem(**workloads.system_kwargs(B.scene_desc(desc, info, k)), device=0) for k in range(2)]
+    b.system.step(40)
+    for s in alone:
+        s.step(40)
+    st = b.scene_stats()
+    p = b.system.read(gg.FIELD_POS)
+    k = np.floor(p[:, 0] / info["width"]).astype(int)
+    for j, s in enumerate(alone):
+        q = p[k == j] - np.array([j * info["width"], 0, 0], np.float32)
+        assert q.shape[0] == s.size() == st[j, 0]
+        assert q.min() >= 0.005 and q.max() <= 0.995
+        ref = s.stats()
+        assert abs(st[j, 5] - ref["kinetic_energy"]) <= 1e-3 * ref["kinetic_energy"] + 1e-9
+    b.close()
+    for s in alone:
+        s.close()
