@@ -44,7 +44,8 @@ constexpr int kMaxSweeps = 2048;  // sweeps per substep (stabilisation + Jacobi)
 
 struct DevScalars {
   unsigned int rmax_bits;      // max contact radius (float bits), this step
-  unsigned int inc_bits[kMaxSweeps];  // per sweep: max |x* increment| (float bits)
+  unsigned int inc_bits[kMaxSweeps];  // per sweep: max |x* increment| per axis (float bits)
+  unsigned int inc_norm_bits[kMaxSweeps];  // per sweep: max Euclidean length of an increment (float bits)
   unsigned int disp0_bits;     // max |dt v| of the predict (float bits)
   unsigned int tile_fallback;  // sweep blocks that could not use the shared-memory tile
   int nl_queued[kMaxSweeps];          // per sweep: particles whose contact list is rebuilt
@@ -293,7 +294,10 @@ gg_status reorder_upsampled(gg_system* S, const uint32_t* perm, cudaStream_t st)
 gg_status radii_all(gg_system* S, cudaStream_t st);
 gg_status predict(gg_system* S, cudaStream_t st);
 gg_status sweep(gg_system* S, int it, cudaStream_t st);
-gg_status apply(gg_system* S, int it, bool stab, bool last, cudaStream_t st);
+// last: write the constraint counts (the substep's last sweep, or every
+// sweep of the residual mode); more: another sweep may follow, so record the
+// per-cell increments its contact lists are checked against.
+gg_status apply(gg_system* S, int it, bool stab, bool last, bool more, cudaStream_t st);
 gg_status finalize(gg_system* S, cudaStream_t st);
 gg_status upsample(gg_system* S, cudaStream_t st);
 gg_status explosion(gg_system* S, float force, cudaStream_t st);

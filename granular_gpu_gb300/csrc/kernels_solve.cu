@@ -108,11 +108,12 @@ struct PlaneArgs {
 __global__ void __launch_bounds__(256) k_apply(int n, float4* __restrict__ xs, float4* __restrict__ pos,
                         const float4* __restrict__ delta, int32_t* __restrict__ s_extra,
                         int32_t* __restrict__ ncon, int32_t* __restrict__ contacts, int stab, int last,
-                        unsigned int* __restrict__ inc_bits, const uint32_t* __restrict__ keys,
+                        unsigned int* __restrict__ inc_bits, unsigned int* __restrict__ inc_norm_bits,
+                        const uint32_t* __restrict__ keys,
                         uint32_t* __restrict__ cell_inc, int C, int nz, UDiv div_z, PlaneArgs pa,
                         const float4* __restrict__ fdelta, float* __restrict__ pn) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  unsigned int bits = 0;
+  unsigned int bits = 0, nbits = 0;
   uint32_t key = 0xffffffffu;
   if (i < n) {
     // every load first, so that they are in flight together
@@ -203,6 +204,9 @@ __global__ void __launch_bounds__(256) k_apply(int n, float4* __restrict__ xs, f
       contacts[i] = c;
     }
     bits = __float_as_uint(fmaxf(fmaxf(fabsf(inc.x), fabsf(inc.y)), fabsf(inc.z)));
+    // the increment's length, rounded up past the roundings of the dot
+    // product and the root (a relative 3e-7 at most)
+    nbits = __float_as_uint(sqrtf(dot3(inc, inc)) * 1.000001f);
   }
   if (cell_inc) {
     // per-cell bound read by the next listed sweep (non-negative float bits
@@ -212,7 +216,7 @@ __global__ void __launch_bounds__(256) k_apply(int n, float4* __restrict__ xs, f
     // of its column), so an entry holds the largest increment over three
     // cells of a column and a stencil needs nine entries, not 27.
     const unsigned peers = __match_any_sync(0xffffffffu, key);
-    const unsigned m = __reduce_max_sync(peers, bits);
+    const unsigned m = __reduce_max_sync(peers, nbits);
     if (key != 0xffffffffu && m && (threadIdx.x & 31) == __ffs(peers) - 1) {
       atomicMax(&cell_inc[key], m);
       if ((int)key < C) {
@@ -223,13 +227,14 @@ __global__ void __launch_bounds__(256) k_apply(int n, float4* __restrict__ xs, f
     }
   }
   block_max_bits_any(inc_bits, bits);
+  block_max_bits_any(inc_norm_bits, nbits);
 }
 
-gg_status apply(gg_system* S, int it, bool stab, bool last, cudaStream_t st) {
+gg_status apply(gg_system* S, int it, bool stab, bool last, bool more, cudaStream_t st) {
   if (S->n <= 0) return GG_OK;
   prof_begin(S, PC_APPLY, st);
-  // the listed sweep after this one reads the per-cell increments
-  uint32_t* cell_inc = (S->g.cell_inc && !last) ? S->g.cell_inc : nullptr;
+  // a listed sweep after this one (more) reads the per-cell increments
+  uint32_t* cell_inc = (S->g.cell_inc && more) ? S->g.cell_inc : nullptr;
   if (cell_inc) GG_CUDA(cudaMemsetAsync(cell_inc, 0, sizeof(uint32_t) * ((size_t)S->grid.C + 1), st));
   PlaneArgs pa;
   pa.n = std::max(0, std::min(S->P.n_planes, 8));
@@ -245,7 +250,8 @@ gg_status apply(gg_system* S, int it, bool stab, bool last, cudaStream_t st) {
   const int ta = S->tune.apply_threads;
   k_apply<<<blocks_for(S->n, ta), ta, 0, st>>>((int)S->n, S->g.xs, S->g.pos[S->g.cur], S->g.delta,
                                                  S->g.s_extra, S->g.ncon, S->g.contacts, stab ? 1 : 0,
-                                                 last ? 1 : 0, &S->scal->inc_bits[it], S->g.keys, cell_inc,
+                                                 last ? 1 : 0, &S->scal->inc_bits[it], &S->scal->inc_norm_bits[it],
+                                                 S->g.keys, cell_inc,
                                                  S->grid.C, S->grid.nz, make_udiv((uint32_t)S->grid.nz), pa,
                                                  pa.coulomb ? S->g.fdelta : nullptr, S->g.pn);
   count_launches(S, 1);

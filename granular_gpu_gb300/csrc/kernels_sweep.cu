@@ -425,16 +425,17 @@ __global__ void __launch_bounds__(kWarpThreads) k_sweep_list(SweepArgs a) {
 //
 // A list built at sweep t stays exact at sweep s while the particle's query
 // cell (hence its stencil) is unchanged and
-//   sqrt(3) * A * 1.0001 + 4 e < skin,   A = sum over sweeps u in [t, s) of 2 (M_u + e),
-// where M_u bounds the per-axis x* increment of sweep u of the particle and
-// of every particle binned in its stencil, and e bounds the rounding of one
-// position update.  A candidate left out was farther than r_i + r_j + skin
-// and has since closed in by less than the skin, so it is still no contact:
-// the corrections, their order and the counts are those of the full scan.
-// M_u is the sweep's global maximum increment when that is small enough,
-// else the largest per-cell maximum (recorded by the apply kernel) over the
-// 27 stencil cells and the particle's own cell.  Lists whose bound runs out
-// are rebuilt by their own thread; the others are kept.
+//   A * 1.0001 + 4 e < skin,   A = sum over sweeps u in [t, s) of 2 (N_u + sqrt(3) e),
+// where N_u bounds the length of the x* increment of sweep u of the particle
+// and of every particle binned in its stencil, and e bounds the rounding of
+// one coordinate's position update.  A candidate left out was farther than
+// r_i + r_j + skin and has since closed in by less than the skin, so it is
+// still no contact: the corrections, their order and the counts are those
+// of the full scan.  N_u is the sweep's global maximum increment length when
+// that is small enough, else the largest per-cell maximum (recorded by the
+// apply kernel) over the 27 stencil cells and the particle's own cell.
+// Lists whose bound runs out are rebuilt by their own thread; the others are
+// kept.
 
 // The listed candidates in order, with the next entry's gathers issued
 // before the current one is processed.  entry(k) gives the k-th entry: a
@@ -473,8 +474,11 @@ __device__ __forceinline__ void apply_entries(const SweepArgs& a, const Target& 
 }
 
 __device__ __forceinline__ bool nlist_bound_ok(const SweepArgs& a, float A) {
-  return 1.7320509f * A * 1.0001f + 4.0f * a.eabs < a.skin;
+  return A * 1.0001f + 4.0f * a.eabs < a.skin;
 }
+
+// One sweep's share of the bound A for an increment-length bound N.
+__device__ __forceinline__ float nlist_step(const SweepArgs& a, float N) { return 2.0f * (N + 1.7320509f * a.eabs); }
 
 // Largest per-cell increment of the last sweep over the stencil of q and the
 // particle's own binning cell.  Every cell_inc entry holds the largest
@@ -528,8 +532,8 @@ __global__ void __launch_bounds__(256, 5) k_sweep_nlist_keep(SweepArgs a) {
     bool keep = false;
     if (m.w >= 0 && m.x == q.x && m.y == q.y && m.z == q.z) {
       const float A0 = a.nl_acc[i];
-      float A = A0 + 2.0f * (__uint_as_float(a.scal->inc_bits[a.it - 1]) + a.eabs);
-      if (!nlist_bound_ok(a, A)) A = A0 + 2.0f * (nlist_cell_bound(a, q, a.keys[i]) + a.eabs);
+      float A = A0 + nlist_step(a, __uint_as_float(a.scal->inc_norm_bits[a.it - 1]));
+      if (!nlist_bound_ok(a, A)) A = A0 + nlist_step(a, nlist_cell_bound(a, q, a.keys[i]));
       if (nlist_bound_ok(a, A)) {
         keep = true;
         a.nl_acc[i] = A;

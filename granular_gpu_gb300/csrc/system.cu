@@ -132,7 +132,7 @@ gg_status step_once(gg_system* S) {
     const int stab = S->P.stab_iters;
     for (int it = 0; it < stab; ++it) {
       if ((rc = sweep(S, it, st)) != GG_OK) return rc;
-      if ((rc = apply(S, it, true, false, st)) != GG_OK) return rc;
+      if ((rc = apply(S, it, true, false, true, st)) != GG_OK) return rc;
     }
     const int cap = std::max(0, std::min(S->P.max_sweeps, kMaxSweeps - stab));
     int k = 0;
@@ -141,7 +141,7 @@ gg_status step_once(gg_system* S) {
       if ((rc = residual(S, st, &res)) != GG_OK) return rc;
       if (!(res > S->P.target_residual) || k >= cap) break;
       if ((rc = sweep(S, stab + k, st)) != GG_OK) return rc;
-      if ((rc = apply(S, stab + k, false, true, st)) != GG_OK) return rc;
+      if ((rc = apply(S, stab + k, false, true, true, st)) != GG_OK) return rc;
       ++k;
     }
     S->last_sweeps = k;
@@ -150,7 +150,7 @@ gg_status step_once(gg_system* S) {
     const int total = std::min(S->P.stab_iters + S->P.iters, kMaxSweeps);
     for (int it = 0; it < total; ++it) {
       if ((rc = sweep(S, it, st)) != GG_OK) return rc;
-      if ((rc = apply(S, it, it < S->P.stab_iters, it == total - 1, st)) != GG_OK) return rc;
+      if ((rc = apply(S, it, it < S->P.stab_iters, it == total - 1, it < total - 1, st)) != GG_OK) return rc;
     }
   }
   if (S->P.warm_start == 2 && (rc = warm_start_target(S, st)) != GG_OK) return rc;

@@ -108,9 +108,9 @@ def test_coulomb_walls_and_coefficients_follow_each_scene():
     desc, info = B.batched_scenes(2, seed=8, lo=2000, hi=4000, law="coulomb")
     b = B.Batch(desc, info)
     alone = [gg.GranularSystem(**workloads.system_kwargs(B.scene_desc(desc, info, k)), device=0) for k in range(2)]
-    b.system.step(40)
+    b.system.step(10)
     for s in alone:
-        s.step(40)
+        s.step(10)
     st = b.scene_stats()
     p = b.system.read(gg.FIELD_POS)
     k = np.floor(p[:, 0] / info["width"]).astype(int)
