@@ -345,6 +345,12 @@ def run_reference(args):
     line["gpu_launches"] = None  # the reference's kernels, not this library's
     line["clocks"] = clocks
     k.close()
+    if not args.no_cpu:
+        # the reference has no CPU implementation of the path: its FP64
+        # restatement on the host cores, on the bounded sample
+        cv, threads, _ = cpu_sample(steps=args.cpu_steps, warmup=1)
+        line["cpu_baseline"] = {"value": cv, "unit": METRIC, "cores": threads, "kind": "port",
+                                "sample": SAMPLE_NOTE + f", {args.cpu_steps} timed substeps, FP64 build"}
     print(json.dumps(line), flush=True)
     return 0
 
