@@ -146,3 +146,61 @@ def test_color_dots_known_answers():
     assert np.array_equal(c[:, 0], np.array([0, 0.34, 0, 0.34], np.float32))
     _, c = orc.color_dots(p, sdist=[0, 5, 100, np.nan], mode=1)
     assert np.array_equal(c, np.array([[0.34, 0.46, 0.7], [1, 0, 0], [0, 0, 0], [1, 0, 0]], np.float32))
+
+
+def _ramp_block_slide(mu):
+    """The oracle's configured mode: a 6 x 4 x 6 block on a 30-degree
+    analytic plane, friction mu / mu; displacement along the slope after
+    60 substeps of 1/240 s, and the deepest centre below the plane."""
+    import math
+    r = 0.01
+    th = math.radians(30.0)
+    t = np.array([math.cos(th), math.sin(th), 0.0])
+    nrm = np.array([-math.sin(th), math.cos(th), 0.0])
+    p0 = np.array([0.5, 0.35, 0.5])
+    pts = [p0 + (i - 2.5) * 2 * r * t + (r * 1.001 + j * 2 * r) * nrm + np.array([0, 0, (k - 2.5) * 2 * r])
+           for i in range(6) for j in range(4) for k in range(6)]
+    p = np.array(pts, np.float32)
+    desc = workloads.box_drop(n_side=2, substeps=4, iters=5, adaptive=0, upsample_per=0)
+    desc.update(particles=p, n_particles=p.shape[0], boundary=np.zeros((0, 3), np.float32), n_boundary=0,
+                skip_initial_step=1)
+    workloads.configure(desc["params"], mu, mu, [(nrm, float(nrm @ p0))])
+    o = orc.OracleSystem(desc, fp64=False)
+    c0 = o.read(abi.FIELD_POS).astype(np.float64).mean(0)
+    o.step(60)
+    x = o.read(abi.FIELD_POS).astype(np.float64)
+    o.close()
+    return float((x.mean(0) - c0) @ t), float((x @ nrm - nrm @ p0).min())
+
+
+def test_configured_friction_on_a_ramp():
+    # the configured mode's Coulomb law in the oracle (the GPU kernels match
+    # it bit for bit, tests/test_configured.py): mu 0.7 > tan 30 holds the
+    # block to a creep, mu 0.1 lets it slide, nothing sinks into the plane
+    free, pen_f = _ramp_block_slide(0.0)
+    stick, pen_s = _ramp_block_slide(0.7)
+    slide, pen_l = _ramp_block_slide(0.1)
+    assert free < -0.12
+    assert abs(stick) < 0.15 * abs(free)
+    assert 0.35 * abs(free) < abs(slide) < 0.7 * abs(free)
+    assert min(pen_f, pen_s, pen_l) > -0.002
+
+
+def test_configured_split_children_claim_their_cells():
+    # heavy isolated surface particles split; with split_claim two parents
+    # never put children in one cell, so no two particles coincide
+    p = workloads.lattice((4, 4, 4), 0.0101, (0.3, 0.3, 0.3), 0.0, 1)
+    desc = workloads.box_drop(n_side=2, substeps=4, iters=3, adaptive=1, upsample_per=0, skip=True)
+    desc.update(particles=p, n_particles=p.shape[0], boundary=np.zeros((0, 3), np.float32), n_boundary=0,
+                gravity=(0.0, 0.0, 0.0))
+    desc["masses"] = np.full(p.shape[0], 4.0, np.float32)
+    workloads.configure(desc["params"], 0.5, 0.4, [])
+    desc["params"].mass_ledger = 1
+    o = orc.OracleSystem(desc, fp64=False)
+    o.step(1)
+    x = o.read(abi.FIELD_POS)
+    n = x.shape[0]
+    assert n > p.shape[0], "the heavy particles must split"
+    d = np.linalg.norm(x[:, None, :] - x[None, :, :], axis=-1) + np.eye(n)
+    assert d.min() > 0.0, "two particles coincide"
+    o.close()
