@@ -946,6 +946,7 @@ gg_status gg_set_tuning(gg_system* S, const gg_tuning* t) {
   REQUIRE(threads_ok(t->predict_threads) && threads_ok(t->apply_threads) && threads_ok(t->finalize_threads) &&
               threads_ok(t->keep_threads),
           "gg_set_tuning: threads per block must be a multiple of 32 in 32..1024");
+  REQUIRE(t->keep_threads <= 256, "gg_set_tuning: keep_threads must be at most 256 (the keep sweep's launch bound)");
   REQUIRE(t->build_blocks_per_sm >= 1 && t->build_blocks_per_sm <= 32,
           "gg_set_tuning: build_blocks_per_sm must be in 1..32");
   REQUIRE(t->sweep_variant == 0 || t->sweep_variant == 1, "gg_set_tuning: sweep_variant must be 0 or 1");

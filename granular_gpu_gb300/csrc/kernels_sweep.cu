@@ -552,14 +552,25 @@ __global__ void __launch_bounds__(256, 5) k_sweep_nlist_keep(SweepArgs a) {
       rebuild = true;
     }
   }
+  // The block's rebuilds go to the queue together, in index order: the
+  // rebuild kernel then takes neighbouring particles into one warp (warps
+  // appending on their own interleave the regions all SMs work on).
+  __shared__ int s_cnt[8], s_base;
   const unsigned bal = __ballot_sync(0xffffffffu, rebuild);
-  if (bal) {
-    const int lane = threadIdx.x & 31;
-    int base = 0;
-    if (lane == 0) base = atomicAdd(&a.scal->nl_queued[a.it], __popc(bal));
-    base = __shfl_sync(0xffffffffu, base, 0);
-    if (rebuild) a.nl_queue[base + __popc(bal & lanemask_lt())] = i;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) s_cnt[w] = __popc(bal);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int tot = 0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
+      const int c = s_cnt[k];
+      s_cnt[k] = tot;
+      tot += c;
+    }
+    s_base = tot ? atomicAdd(&a.scal->nl_queued[a.it], tot) : 0;
   }
+  __syncthreads();
+  if (rebuild) a.nl_queue[s_base + s_cnt[w] + __popc(bal & lanemask_lt())] = i;
 }
 
 // List build: scan the 27 cells in the reference order, write the
