@@ -254,6 +254,11 @@ struct MergeArgs {
 
 // merge_mark_gpu (Solver.cu:526-653), scan phase: every thread's neighbour
 // scan sees remove[] as it was at kernel start.
+// ALL: the merge radius reaches past every candidate of the stencil (the
+// reference's 0.035 at r = 0.002), so the chunk masks would mark nearly all
+// of them: every candidate is visited, in the same order, and the exact
+// radius test alone decides, as in the masked form.
+template <bool ALL>
 __global__ void __launch_bounds__(256) k_merge_scan(MergeArgs a) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.n) return;
@@ -286,10 +291,14 @@ __global__ void __launch_bounds__(256) k_merge_scan(MergeArgs a) {
       // the chunk's mask marks the others, visited in candidate order
       const int cn = min(32, j1 - c0);
       unsigned mask = 0u;
+      if (ALL) {
+        mask = cn == 32 ? 0xffffffffu : (1u << cn) - 1u;
+      } else {
 #pragma unroll 4
-      for (int b = 0; b < cn; ++b) {
-        const float3 d = sub3(xi, f3(a.pos[c0 + b]));
-        mask |= (__fmaf_rn(d.x, d.x, __fmaf_rn(d.y, d.y, __fmul_rn(d.z, d.z))) > pre_cut ? 0u : 1u) << b;
+        for (int b = 0; b < cn; ++b) {
+          const float3 d = sub3(xi, f3(a.pos[c0 + b]));
+          mask |= (__fmaf_rn(d.x, d.x, __fmaf_rn(d.y, d.y, __fmul_rn(d.z, d.z))) > pre_cut ? 0u : 1u) << b;
+        }
       }
       while (mask) {
         const int j = c0 + __ffs(mask) - 1;
@@ -496,7 +505,12 @@ gg_status merge_mark(gg_system* S, cudaStream_t st) {
   }
   const int nb = blocks_for(S->n, 256);
   prof_begin(S, PC_MERGE, st);
-  k_merge_scan<<<nb, 256, 0, st>>>(a);
+  // every candidate of a stencil lies within sqrt(12) cell lengths of the
+  // particle, plus what it moved since the grid was built (the predicted
+  // step and the sweeps; the ALL form stays exact either way)
+  const float reach2 = 12.0f * S->grid.L * S->grid.L * 1.001f;
+  if (reach2 < a.merge_r2_cut) k_merge_scan<true><<<nb, 256, 0, st>>>(a);
+  else k_merge_scan<false><<<nb, 256, 0, st>>>(a);
   k_merge_claims<<<nb, 256, 0, st>>>(a);
   {
     void* args[] = {&a};
