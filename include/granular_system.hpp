@@ -236,6 +236,13 @@ class GranularSystem {
   std::vector<float> frame_times_;
 };
 
+// updateAnimation (main.cu:1210-1277) with the animation state passed in
+// instead of main.cu's global AnimationState; call it once per frame before
+// the frame's steps.  The state of a scene comes from gg_scene_animation.
+inline void updateAnimation(GranularSystem& sys, gg_animation& state, float dt) {
+  gg_shim::check(gg_update_animation(sys.handle(), &state, dt));
+}
+
 // generate_dots (VBO.hpp:96-106) over device buffers instead of mapped
 // OpenGL buffer objects: positions and colours of the set as float3, the
 // colour chosen by show_surface (0 surface flag, 1 surface distance, 2 mass
