@@ -109,3 +109,25 @@ def test_noalloc_grid_build_checks_its_limits_before_touching_a_gpu():
                                    C.c_void_p(16), C.c_void_p(16), C.c_void_p(16), None)
     assert rc == abi.GG_ERR_CAPACITY
     assert b"262144" in lib.gg_last_error()
+
+
+def test_new_entry_points_check_their_arguments_without_a_gpu():
+    lib = gg.lib()
+    # batched scenes in configured mode, animated walls: null systems and
+    # states are refused with a message, before any device work
+    mu = (C.c_float * 2)(0.5, 0.6)
+    assert lib.gg_set_scene_coulomb(None, 2, mu, mu) == abi.GG_ERR_INVALID_ARGUMENT
+    assert b"gg_set_scenes" in lib.gg_last_error()
+    assert lib.gg_update_animation(None, None, C.c_float(0.1)) == abi.GG_ERR_INVALID_ARGUMENT
+    assert lib.gg_animate_walls(None, None) == abi.GG_ERR_INVALID_ARGUMENT
+    assert lib.gg_animation_advance(None, C.c_float(0.1), None, 0, None) == abi.GG_ERR_INVALID_ARGUMENT
+    assert lib.gg_default_animation(None) == abi.GG_ERR_INVALID_ARGUMENT
+    a = abi.gg_animation()
+    assert lib.gg_scene_animation(None, None, C.byref(a)) == abi.GG_ERR_INVALID_ARGUMENT
+    assert lib.gg_scene_animation(b"/nonexistent/scene.json", None, C.byref(a)) == abi.GG_ERR_IO
+    assert lib.gg_animation_needs_centroid(None, C.c_float(0.1)) == 0
+    # a state that is not animating moves nothing and needs nothing
+    assert lib.gg_default_animation(C.byref(a)) == abi.GG_OK
+    m = abi.gg_animation_move()
+    assert lib.gg_animation_advance(C.byref(a), C.c_float(0.1), None, 0, C.byref(m)) == abi.GG_OK
+    assert m.apply == 0 and a.animation_time == 0.0
