@@ -632,7 +632,7 @@ def run_mine(args):
         # integer ledger, 4 render points per particle; timed after 100
         # substeps (merges under way)
         line["adaptive_pile"] = pile_rate(local, args.pile_steps)
-    if rank == 0 and world == 1 and not args.no_pile:
+    if rank == 0 and world == 1 and not args.no_box:
         # the box-drop configuration as stated (Coulomb friction 0.5 / 0.4)
         line["box_drop_configured"] = box_drop_rate(local)
     if rank == 0 and world == 1 and not args.no_batched:
@@ -727,6 +727,7 @@ def main():
     ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-pile", action="store_true")
+    ap.add_argument("--no-box", action="store_true", help="skip the box-drop configuration (Coulomb friction)")
     ap.add_argument("--no-scaled", action="store_true")
     ap.add_argument("--pile-steps", type=int, default=60)
     ap.add_argument("--batched-frames", type=int, default=10)
